@@ -1,0 +1,168 @@
+"""ORACLE — test infrastructure only.
+
+CPU restatement of the reference's Generate/Solve path (GetDP 3.5.0 element
+loop + Sparskit backend) used to check the GPU product.  Only the tests,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may load
+it, and only as the checker; the product never routes through it.
+
+The C sources next to this file are compiled into ``oracle/_build`` by
+:func:`build` (two flavours: double-precision ILU, and single-precision ILU
+as in the official reference build, ``HAVE_ILU_FLOAT``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+SOURCES = ["sparskit_port.c", "solve_port.c", "assemble_port.c"]
+_LIBS: dict = {}
+
+# Sparskit.h codes
+CG, GMRES, FGMRES = 1, 8, 9
+NONE, ILU0, DIAGONAL = 0, 6, 8
+
+
+def _lib_path(ilu: str) -> str:
+    return os.path.join(BUILD, f"liboracle_ilu{ilu}.so")
+
+
+def build(force: bool = False) -> None:
+    """Compile both oracle flavours (a few seconds with gcc)."""
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
+    newest = max(os.path.getmtime(s) for s in srcs)
+    for ilu, flag in (("64", []), ("32", ["-DHAVE_ILU_FLOAT"])):
+        out = _lib_path(ilu)
+        if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
+            continue
+        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w",
+               *flag, *srcs, "-o", out, "-lm"]
+        subprocess.check_call(cmd)
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("algorithm", ctypes.c_int), ("preconditioner", ctypes.c_int),
+                ("precond_position", ctypes.c_int), ("scaling", ctypes.c_int),
+                ("renumbering", ctypes.c_int), ("krylov_size", ctypes.c_int),
+                ("nb_iter_max", ctypes.c_int), ("stopping_test", ctypes.c_double)]
+
+
+def lib(ilu: str = "64") -> ctypes.CDLL:
+    if ilu not in _LIBS:
+        path = _lib_path(ilu)
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        i64, i32p, dp = ctypes.c_int64, ctypes.POINTER(ctypes.c_int32), \
+            ctypes.POINTER(ctypes.c_double)
+        L.oracle_assemble_tri_p1.restype = i64
+        L.oracle_assemble_tet10_elasticity.restype = i64
+        L.oracle_assemble_tet4_curlcurl.restype = i64
+        L.oracle_coo_to_csr.restype = i64
+        L.oracle_solve_csr.restype = ctypes.c_int
+        _LIBS[ilu] = L
+    return _LIBS[ilu]
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def assemble(problem, dofmap, ilu: str = "64"):
+    """Run the restated element loop; returns (indptr, indices, data, b)."""
+    L = lib(ilu)
+    m = problem.mesh
+    n = dofmap.n_dof
+    ne = m.n_elems
+    nodes = np.ascontiguousarray(m.nodes, np.float64)
+    elems = np.ascontiguousarray(m.elems, np.int32)
+    edofs = np.ascontiguousarray(dofmap.elem_dofs, np.int32)
+    nloc = edofs.shape[1]
+    f = problem.formulation
+    cap = ne * nloc * nloc * (4 if f == "eddy2d" else 1) * 2
+    rr = np.empty(cap, np.int32)
+    cc = np.empty(cap, np.int32)
+    vv = np.empty(cap, np.float64)
+    b = np.zeros(n, np.float64)
+    I32, D = ctypes.c_int32, ctypes.c_double
+    if f in ("magnetostatics2d", "eddy2d"):
+        cplx = f == "eddy2d"
+        sigma = np.ascontiguousarray(problem.params.get("sigma", np.zeros(ne)), np.float64)
+        omega = problem.params.get("freq", 0.0) * 6.2831853071795865
+        nz = L.oracle_assemble_tri_p1(
+            ne, _p(nodes, D), _p(elems, ctypes.c_int), _p(edofs, ctypes.c_int),
+            _p(np.ascontiguousarray(problem.coef, np.float64), D),
+            _p(np.ascontiguousarray(problem.source, np.float64), D),
+            _p(sigma, D), ctypes.c_double(omega), int(cplx), ctypes.c_int64(cap),
+            _p(rr, I32), _p(cc, I32), _p(vv, D), _p(b, D))
+    elif f == "elasticity":
+        fz = -problem.params["rho"] * problem.params["g"]
+        nz = L.oracle_assemble_tet10_elasticity(
+            ne, _p(nodes, D), _p(elems, ctypes.c_int), _p(edofs, ctypes.c_int),
+            _p(np.ascontiguousarray(problem.coef, np.float64), D),
+            ctypes.c_double(problem.params["poisson"]), ctypes.c_double(fz),
+            ctypes.c_int64(cap), _p(rr, I32), _p(cc, I32), _p(vv, D), _p(b, D))
+    elif f == "curlcurl":
+        sg = np.ascontiguousarray(dofmap.elem_sign, np.int8)
+        nz = L.oracle_assemble_tet4_curlcurl(
+            ne, _p(nodes, D), _p(elems, ctypes.c_int), _p(edofs, ctypes.c_int),
+            _p(sg, ctypes.c_byte),
+            _p(np.ascontiguousarray(problem.coef, np.float64), D),
+            _p(np.ascontiguousarray(problem.source, np.float64), D),
+            ctypes.c_double(problem.params["reg"]), ctypes.c_double(problem.params["J0"]),
+            ctypes.c_int64(cap), _p(rr, I32), _p(cc, I32), _p(vv, D), _p(b, D))
+    else:
+        raise ValueError(f)
+    if nz > cap:
+        raise RuntimeError("oracle COO capacity exceeded")
+    indptr = np.empty(n + 1, np.int32)
+    indices = np.empty(nz, np.int32)
+    data = np.empty(nz, np.float64)
+    nnz = L.oracle_coo_to_csr(n, ctypes.c_int64(nz), _p(rr, I32), _p(cc, I32),
+                              _p(vv, D), _p(indptr, I32), _p(indices, I32),
+                              _p(data, D))
+    return indptr, indices[:nnz].copy(), data[:nnz].copy(), b
+
+
+def solve(indptr, indices, data, b, algorithm=GMRES, preconditioner=ILU0,
+          scaling=0, renumbering=1, krylov_size=40, nb_iter_max=1000,
+          stopping_test=1e-10, precond_position=2, ilu: str = "64"):
+    """Restated Sparskit solve_matrix; returns (x, status, iterations, res)."""
+    L = lib(ilu)
+    n = len(indptr) - 1
+    p = _Params(algorithm, preconditioner, precond_position, scaling,
+                renumbering, krylov_size, nb_iter_max, stopping_test)
+    x = np.zeros(n, np.float64)
+    its = ctypes.c_int(0)
+    res = ctypes.c_double(0.0)
+    ip = np.ascontiguousarray(indptr, np.int32)
+    ix = np.ascontiguousarray(indices, np.int32)
+    dv = np.ascontiguousarray(data, np.float64)
+    bv = np.ascontiguousarray(b, np.float64)
+    st = L.oracle_solve_csr(n, _p(ip, ctypes.c_int), _p(ix, ctypes.c_int),
+                            _p(dv, ctypes.c_double), _p(bv, ctypes.c_double),
+                            _p(x, ctypes.c_double), ctypes.byref(p),
+                            ctypes.byref(its), ctypes.byref(res))
+    return x, st, its.value, res.value
+
+
+def params_from_golden(keys, vals) -> dict:
+    """solver.par keys (as stored in the golden fixtures) -> solve() kwargs."""
+    m = {"Algorithm": "algorithm", "Preconditioner": "preconditioner",
+         "Scaling": "scaling", "Renumbering_Technique": "renumbering",
+         "Krylov_Size": "krylov_size", "Nb_Iter_Max": "nb_iter_max",
+         "Stopping_Test": "stopping_test"}
+    out = {}
+    for k, v in zip(keys, vals):
+        k = str(k)
+        out[m[k]] = float(v) if k == "Stopping_Test" else int(v)
+    # reference defaults (Sparskit.cpp:1847-1868) for keys not given
+    out.setdefault("krylov_size", 40)
+    out.setdefault("scaling", 0)
+    out.setdefault("renumbering", 1)
+    return out
