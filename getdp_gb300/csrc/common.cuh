@@ -1,0 +1,159 @@
+// Shared infrastructure of the GB300 backend: error reporting, the context
+// (one device, one stream), device buffers and small device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/getdp_gb300.h"
+
+namespace gb {
+
+struct ilu_data;
+
+// last error message, per thread (read through gb300_last_error)
+void set_error(const char *fmt, ...);
+
+#define GB_CUDA(x)                                                           \
+  do {                                                                       \
+    cudaError_t e_ = (x);                                                    \
+    if(e_ != cudaSuccess) {                                                  \
+      ::gb::set_error("%s:%d: %s failed: %s", __FILE__, __LINE__, #x,        \
+                      cudaGetErrorString(e_));                               \
+      return GB300_ERR_CUDA;                                                 \
+    }                                                                        \
+  } while(0)
+
+#define GB_TRY(...)                                                          \
+  do {                                                                       \
+    int r_ = (__VA_ARGS__);                                                  \
+    if(r_ != GB300_OK) return r_;                                            \
+  } while(0)
+
+// number of SMs on GB300 and the partial-sum grid used by every
+// deterministic reduction (fixed, so results do not depend on timing)
+constexpr int kReduceBlocks = 1216;  // 152 SMs x 8
+constexpr int kReduceThreads = 256;
+
+template <typename T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release()
+  {
+    if(p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  int alloc(size_t count)
+  {
+    if(count <= n && p) return GB300_OK;
+    release();
+    if(count == 0) return GB300_OK;
+    cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+    if(e != cudaSuccess) {
+      set_error("cudaMalloc(%zu bytes) failed: %s", count * sizeof(T),
+                cudaGetErrorString(e));
+      p = nullptr;
+      return GB300_ERR_CUDA;
+    }
+    n = count;
+    return GB300_OK;
+  }
+};
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+  for(int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v)
+{
+  for(int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block-wide sum in a fixed order; result valid in thread 0
+template <typename T, int NT> __device__ __forceinline__ T block_sum(T v)
+{
+  __shared__ T red[NT / 32];
+  v = warp_sum(v);
+  if((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  T s = 0;
+  if(threadIdx.x == 0)
+    for(int w = 0; w < NT / 32; w++) s += red[w];
+  __syncthreads();
+  return s;
+}
+
+// streaming loads for data read once per pass (matrix values and indices)
+template <typename T> __device__ __forceinline__ T ld_stream(const T *p)
+{
+  return __ldcs(p);
+}
+
+// position of column c in the sorted row [lo, hi) of col[], or -1
+__device__ __forceinline__ int find_col(const int *__restrict__ col, int lo,
+                                        int hi, int c)
+{
+  const int end = hi;
+  while(lo < hi) {
+    int mid = (lo + hi) >> 1;
+    int v = col[mid];
+    if(v < c)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return (lo < end && col[lo] == c) ? lo : -1;
+}
+
+inline int grid_for(long long work, int threads, int max_blocks = 1 << 30)
+{
+  long long b = (work + threads - 1) / threads;
+  if(b < 1) b = 1;
+  if(b > max_blocks) b = max_blocks;
+  return (int)b;
+}
+
+}  // namespace gb
+
+// the objects behind the opaque handles of the C ABI
+struct gb300_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 152;
+};
+
+struct gb300_vector {
+  gb300_ctx *ctx = nullptr;
+  int n = 0;
+  gb::DevBuf<double> d;
+};
+
+struct gb300_matrix {
+  gb300_ctx *ctx = nullptr;
+  int n = 0;
+  // host staging of LinAlg-style scalar adds, in call order
+  std::vector<int> hr, hc;
+  std::vector<double> hv;
+  // device CSR (0-based, rows sorted by column)
+  gb::DevBuf<int> rowptr, col;
+  gb::DevBuf<double> val;
+  gb::DevBuf<float> val32;  // fp32 copy for mixed-precision inner solves
+  long long nnz = 0;
+  bool csr_valid = false;
+  bool val32_valid = false;
+  int tpr = 32;  // threads per row for the CSR kernels
+  // ILU(0) state, created on demand by the solver
+  gb::ilu_data *ilu = nullptr;
+};

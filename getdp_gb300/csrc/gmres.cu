@@ -1,0 +1,809 @@
+// ILU(0) and the GMRES family on the GPU.
+//
+// ILU(0) (ilu0, contrib/Sparskit/ilut.F:1818-1941) keeps A's pattern; the
+// factor is stored in a copy of A's values (L multipliers left of the
+// diagonal, U right of it) plus the inverted pivots, as Sparskit's MSR
+// layout does.  Rows are factored and solved level by level: a level holds
+// rows whose lower (resp. upper) neighbours all belong to earlier levels,
+// so its rows are independent.  Narrow levels (<= kNarrow rows) run back to
+// back inside one thread block separated by __syncthreads; a wide level gets
+// its own grid launch.  The triangular solves follow lusol
+// (ilut.F:2297-2347) row by row in the same accumulation order.
+//
+// GMRES(m) and FGMRES(m) follow iters.f:1912-2219 / :2522-2806 with right
+// preconditioning (Preconditioner_Position 2): restart residual, Arnoldi
+// steps, Givens rotations (iters.f:3235-3273), the stopping test on the
+// Givens residual estimate, and the triangular solve + update at the end of
+// a cycle.  The orthogonalisation is classical Gram-Schmidt applied twice
+// (two passes of block dot products), which parallelises over the basis,
+// in place of the reference's sequential modified Gram-Schmidt with
+// selective re-orthogonalisation (mgsro, iters.f:3475); both return an
+// orthonormal basis to working precision.
+#include "krylov.cuh"
+
+namespace gb {
+
+constexpr int kNarrow = 2048;
+constexpr int kNarrowThreads = 1024;
+
+struct Segment {
+  int l0, l1;  // levels [l0, l1)
+  bool narrow;
+  int width;   // rows of the (single) wide level
+  int r0;      // first index in the level-row list
+};
+
+struct ilu_data {
+  int n = 0;
+  DevBuf<int> diag;                 // position of a_ii in each row
+  DevBuf<int> lrows, urows;         // rows grouped by level
+  DevBuf<int> lptr, uptr;           // level offsets (device copies)
+  std::vector<int> hlptr, huptr;    // level offsets (host)
+  std::vector<Segment> lseg, useg;
+  DevBuf<double> lu64, inv64;
+  DevBuf<float> lu32, inv32;
+  bool fact64 = false, fact32 = false;
+};
+
+void ilu_free(ilu_data *d) { delete d; }
+
+// ---------------------------------------------------------------------------
+// level schedule
+// ---------------------------------------------------------------------------
+__global__ void k_ilu_prep(int n, const int *__restrict__ rowptr,
+                           const int *__restrict__ col, int *__restrict__ diag,
+                           int *__restrict__ indl, int *__restrict__ indu,
+                           int *__restrict__ err)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= n) return;
+  int s = rowptr[i], e = rowptr[i + 1];
+  int dpos = -1, nl = 0, nu = 0;
+  for(int k = s; k < e; k++) {
+    int c = col[k];
+    if(c < i)
+      nl++;
+    else if(c > i)
+      nu++;
+    else
+      dpos = k;
+    // structural symmetry: (c, i) must exist
+    if(c != i && find_col(col, rowptr[c], rowptr[c + 1], i) < 0)
+      atomicOr(err, 2);
+  }
+  if(dpos < 0) atomicOr(err, 1);
+  diag[i] = dpos;
+  indl[i] = nl;
+  indu[i] = nu;
+}
+
+__global__ void k_level0(int n, const int *__restrict__ indeg,
+                         int *__restrict__ rows, int *__restrict__ cnt)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i < n && indeg[i] == 0) rows[atomicAdd(cnt, 1)] = i;
+}
+
+// release the dependants of one level; UPPER = 0 walks the lower
+// triangular DAG (dependants of i are j > i in row i), UPPER = 1 the upper
+template <int UPPER>
+__global__ void k_level_next(int p0, int p1, const int *__restrict__ rowptr,
+                             const int *__restrict__ col,
+                             const int *__restrict__ diag,
+                             int *__restrict__ indeg, int *__restrict__ rows,
+                             int *__restrict__ cnt)
+{
+  int t = p0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if(t >= p1) return;
+  int i = rows[t];
+  int s = UPPER ? rowptr[i] : diag[i] + 1;
+  int e = UPPER ? diag[i] : rowptr[i + 1];
+  for(int k = s; k < e; k++) {
+    int j = col[k];
+    if(atomicSub(&indeg[j], 1) == 1) rows[p1 + atomicAdd(cnt, 1)] = j;
+  }
+}
+
+template <int UPPER>
+static int make_levels(gb300_matrix *A, ilu_data *L, int *d_indeg,
+                       DevBuf<int> &rows, DevBuf<int> &dptr,
+                       std::vector<int> &hptr, std::vector<Segment> &seg)
+{
+  cudaStream_t st = A->ctx->stream;
+  int n = A->n;
+  DevBuf<int> cnt;
+  GB_TRY(cnt.alloc(1));
+  GB_TRY(rows.alloc(n));
+  GB_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int), st));
+  k_level0<<<grid_for(n, 256), 256, 0, st>>>(n, d_indeg, rows.p, cnt.p);
+  int c = 0;
+  GB_CUDA(cudaMemcpyAsync(&c, cnt.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  hptr.assign(1, 0);
+  hptr.push_back(c);
+  int p0 = 0, p1 = c;
+  while(p1 < n) {
+    if(p1 == p0) {
+      set_error("ILU level schedule: dependency cycle");
+      return GB300_ERR_ARG;
+    }
+    GB_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int), st));
+    k_level_next<UPPER><<<grid_for(p1 - p0, 256), 256, 0, st>>>(
+      p0, p1, A->rowptr.p, A->col.p, L->diag.p, d_indeg, rows.p, cnt.p);
+    GB_CUDA(cudaMemcpyAsync(&c, cnt.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    p0 = p1;
+    p1 += c;
+    hptr.push_back(p1);
+  }
+  int nl = (int)hptr.size() - 1;
+  GB_TRY(dptr.alloc(nl + 1));
+  GB_CUDA(cudaMemcpyAsync(dptr.p, hptr.data(), sizeof(int) * (nl + 1),
+                          cudaMemcpyHostToDevice, st));
+  seg.clear();
+  for(int l = 0; l < nl;) {
+    int w = hptr[l + 1] - hptr[l];
+    if(w > kNarrow) {
+      seg.push_back({l, l + 1, false, w, hptr[l]});
+      l++;
+    }
+    else {
+      int l1 = l;
+      while(l1 < nl && hptr[l1 + 1] - hptr[l1] <= kNarrow) l1++;
+      seg.push_back({l, l1, true, 0, hptr[l]});
+      l = l1;
+    }
+  }
+  GB_CUDA(cudaStreamSynchronize(st));
+  return GB300_OK;
+}
+
+static int ilu_setup(gb300_matrix *A)
+{
+  if(A->ilu && A->ilu->n == A->n) return GB300_OK;
+  if(A->ilu) ilu_free(A->ilu);
+  A->ilu = new ilu_data();
+  ilu_data *L = A->ilu;
+  L->n = A->n;
+  cudaStream_t st = A->ctx->stream;
+  int n = A->n;
+  DevBuf<int> indl, indu, err;
+  GB_TRY(L->diag.alloc(n));
+  GB_TRY(indl.alloc(n));
+  GB_TRY(indu.alloc(n));
+  GB_TRY(err.alloc(1));
+  GB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+  k_ilu_prep<<<grid_for(n, 256), 256, 0, st>>>(n, A->rowptr.p, A->col.p,
+                                                L->diag.p, indl.p, indu.p, err.p);
+  int herr = 0;
+  GB_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if(herr & 1) {
+    set_error("ILU(0): a row has no diagonal entry");
+    ilu_free(A->ilu);
+    A->ilu = nullptr;
+    return GB300_ERR_ZERO_PIVOT;
+  }
+  if(herr & 2) {
+    set_error("ILU(0): the level schedule needs a structurally symmetric pattern");
+    ilu_free(A->ilu);
+    A->ilu = nullptr;
+    return GB300_ERR_UNSUPPORTED;
+  }
+  int rc = make_levels<0>(A, L, indl.p, L->lrows, L->lptr, L->hlptr, L->lseg);
+  if(rc == GB300_OK)
+    rc = make_levels<1>(A, L, indu.p, L->urows, L->uptr, L->huptr, L->useg);
+  if(rc != GB300_OK) {
+    ilu_free(A->ilu);
+    A->ilu = nullptr;
+  }
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// per-row work of the three level-scheduled sweeps
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void row_fact(int i, const int *__restrict__ rowptr,
+                                         const int *__restrict__ col,
+                                         const int *__restrict__ diag, T *lu,
+                                         T *inv, int *zero_row)
+{
+  int s = rowptr[i], e = rowptr[i + 1], di = diag[i];
+  for(int k = s; k < di; k++) {
+    int kr = col[k];
+    T l = lu[k] * inv[kr];  // tl = alu(j) * alu(jrow)
+    lu[k] = l;
+    int ks = diag[kr] + 1, ke = rowptr[kr + 1];
+    int lo = k + 1;  // columns of row i beyond kr
+    for(int kk = ks; kk < ke; kk++) {
+      int c = col[kk];
+      int pos = find_col(col, lo, e, c);
+      if(pos >= 0) {
+        lu[pos] = lu[pos] - l * lu[kk];
+        lo = pos + 1;
+      }
+    }
+  }
+  T piv = lu[di];
+  if(piv == (T)0) {
+    atomicMin(zero_row, i + 1);
+    inv[i] = (T)0;
+  }
+  else
+    inv[i] = (T)(1.0 / (double)piv);
+}
+
+template <typename T>
+__device__ __forceinline__ void row_fwd(int i, const int *__restrict__ rowptr,
+                                        const int *__restrict__ col,
+                                        const int *__restrict__ diag,
+                                        const T *__restrict__ lu, T *x)
+{
+  T s = x[i];
+  for(int k = rowptr[i]; k < diag[i]; k++) s = s - lu[k] * x[col[k]];
+  x[i] = s;
+}
+
+template <typename T>
+__device__ __forceinline__ void row_bwd(int i, const int *__restrict__ rowptr,
+                                        const int *__restrict__ col,
+                                        const int *__restrict__ diag,
+                                        const T *__restrict__ lu,
+                                        const T *__restrict__ inv, T *x)
+{
+  T s = x[i];
+  for(int k = diag[i] + 1; k < rowptr[i + 1]; k++) s = s - lu[k] * x[col[k]];
+  x[i] = inv[i] * s;
+}
+
+// MODE 0 factor, 1 forward solve, 2 backward solve
+template <int MODE, typename T>
+__global__ void __launch_bounds__(kNarrowThreads)
+k_levels_narrow(int l0, int l1, const int *__restrict__ lptr,
+                const int *__restrict__ rows, const int *__restrict__ rowptr,
+                const int *__restrict__ col, const int *__restrict__ diag,
+                T *lu, T *inv, T *x, int *zero_row, const int *flag)
+{
+  if(flag && !*flag) return;
+  for(int l = l0; l < l1; l++) {
+    int a = lptr[l], b = lptr[l + 1];
+    for(int t = a + threadIdx.x; t < b; t += blockDim.x) {
+      int i = rows[t];
+      if(MODE == 0)
+        row_fact<T>(i, rowptr, col, diag, lu, inv, zero_row);
+      else if(MODE == 1)
+        row_fwd<T>(i, rowptr, col, diag, lu, x);
+      else
+        row_bwd<T>(i, rowptr, col, diag, lu, inv, x);
+    }
+    __syncthreads();
+  }
+}
+
+template <int MODE, typename T>
+__global__ void __launch_bounds__(256)
+k_level_wide(int r0, int width, const int *__restrict__ rows,
+             const int *__restrict__ rowptr, const int *__restrict__ col,
+             const int *__restrict__ diag, T *lu, T *inv, T *x, int *zero_row,
+             const int *flag)
+{
+  if(flag && !*flag) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if(t >= width) return;
+  int i = rows[r0 + t];
+  if(MODE == 0)
+    row_fact<T>(i, rowptr, col, diag, lu, inv, zero_row);
+  else if(MODE == 1)
+    row_fwd<T>(i, rowptr, col, diag, lu, x);
+  else
+    row_bwd<T>(i, rowptr, col, diag, lu, inv, x);
+}
+
+template <int MODE, typename T>
+static void run_levels(const gb300_matrix *A, const ilu_data *L, T *lu, T *inv,
+                       T *x, int *zero_row, const int *flag, cudaStream_t st)
+{
+  bool upper = (MODE == 2);
+  const std::vector<Segment> &seg = upper ? L->useg : L->lseg;
+  const int *rows = upper ? L->urows.p : L->lrows.p;
+  const int *lptr = upper ? L->uptr.p : L->lptr.p;
+  for(const Segment &s : seg) {
+    if(s.narrow)
+      k_levels_narrow<MODE, T><<<1, kNarrowThreads, 0, st>>>(
+        s.l0, s.l1, lptr, rows, A->rowptr.p, A->col.p, L->diag.p, lu, inv, x,
+        zero_row, flag);
+    else
+      k_level_wide<MODE, T><<<grid_for(s.width, 256), 256, 0, st>>>(
+        s.r0, s.width, rows, A->rowptr.p, A->col.p, L->diag.p, lu, inv, x,
+        zero_row, flag);
+  }
+}
+
+template <typename TO, typename TI>
+__global__ void k_cvt(long long n, const TI *__restrict__ in, TO *__restrict__ out,
+                      const int *flag)
+{
+  if(flag && !*flag) return;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if(i < n) out[i] = (TO)in[i];
+}
+
+// factor A's values (val) into the ILU(0) of the requested precision
+static int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out)
+{
+  GB_TRY(ilu_setup(A));
+  ilu_data *L = A->ilu;
+  cudaStream_t st = A->ctx->stream;
+  int n = A->n;
+  DevBuf<int> zr;
+  GB_TRY(zr.alloc(1));
+  int big = 0x7fffffff;
+  GB_CUDA(cudaMemcpyAsync(zr.p, &big, sizeof(int), cudaMemcpyHostToDevice, st));
+  if(!fp32) {
+    GB_TRY(L->lu64.alloc(A->nnz));
+    GB_TRY(L->inv64.alloc(n));
+    GB_CUDA(cudaMemcpyAsync(L->lu64.p, val, sizeof(double) * A->nnz,
+                            cudaMemcpyDeviceToDevice, st));
+    run_levels<0, double>(A, L, L->lu64.p, L->inv64.p, (double *)nullptr, zr.p,
+                          nullptr, st);
+  }
+  else {
+    GB_TRY(L->lu32.alloc(A->nnz));
+    GB_TRY(L->inv32.alloc(n));
+    k_cvt<float, double><<<grid_for(A->nnz, 256), 256, 0, st>>>(A->nnz, val,
+                                                                L->lu32.p, nullptr);
+    run_levels<0, float>(A, L, L->lu32.p, L->inv32.p, (float *)nullptr, zr.p,
+                         nullptr, st);
+  }
+  int hz = 0;
+  GB_CUDA(cudaMemcpyAsync(&hz, zr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  GB_CUDA(cudaGetLastError());
+  *zero_row_out = (hz == big) ? 0 : hz;
+  return GB300_OK;
+}
+
+// z = M^-1 v for the ILU(0) factor (double or float work precision)
+static void ilu_apply(const gb300_matrix *A, bool fp32, const double *v,
+                      double *z, float *t32, const int *flag, cudaStream_t st)
+{
+  const ilu_data *L = A->ilu;
+  int n = A->n;
+  if(!fp32) {
+    if(v != z)
+      k_cvt<double, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, z, flag);
+    run_levels<1, double>(A, L, (double *)L->lu64.p, (double *)L->inv64.p, z,
+                          nullptr, flag, st);
+    run_levels<2, double>(A, L, (double *)L->lu64.p, (double *)L->inv64.p, z,
+                          nullptr, flag, st);
+  }
+  else {
+    k_cvt<float, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, t32, flag);
+    run_levels<1, float>(A, L, (float *)L->lu32.p, (float *)L->inv32.p, t32,
+                         nullptr, flag, st);
+    run_levels<2, float>(A, L, (float *)L->lu32.p, (float *)L->inv32.p, t32,
+                         nullptr, flag, st);
+    k_cvt<double, float><<<grid_for(n, 256), 256, 0, st>>>(n, t32, z, flag);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GMRES device state and kernels
+// ---------------------------------------------------------------------------
+constexpr int kMaxKrylov = 128;
+
+struct GmState {
+  int active;       // whole solve still running
+  int cycle;        // current restart cycle still extending the basis
+  int did_cycle;    // the cycle took >= 1 Arnoldi step (solution update due)
+  int k;            // Arnoldi steps taken in the cycle
+  int its;          // ipar(7)
+  int maxit;        // ipar(6)
+  int status;       // ipar(1)
+  int breakdown;    // ipar(12) (-3: linear combination, -1/-2 bad vector)
+  int first;        // first restart still to come
+  double tol;       // fpar(4)
+  double res0;      // fpar(3)
+  double res;       // fpar(5)
+  double res6;      // fpar(6)
+  double rtol;
+  double scale;     // 1 / h(k+1,k) for the new basis vector
+  double H[(kMaxKrylov + 1) * kMaxKrylov];  // column-major, (m+1) x m
+  double cs[kMaxKrylov], sn[kMaxKrylov], g[kMaxKrylov + 1], y[kMaxKrylov];
+  double h1[kMaxKrylov + 1], h2[kMaxKrylov + 1];
+};
+
+__device__ void givens_dev(double *x, double *y, double *c, double *s)
+{
+  if(*x == 0. && *y == 0.) {
+    *c = 1.;
+    *s = 0.;
+  }
+  else if(fabs(*y) > fabs(*x)) {
+    double t = *x / *y;
+    *x = sqrt(1. + t * t);
+    *s = copysign(1. / *x, *y);
+    *c = t * *s;
+  }
+  else if(fabs(*y) <= fabs(*x)) {
+    double t = *y / *x;
+    *y = sqrt(1. + t * t);
+    *c = copysign(1. / *y, *x);
+    *s = t * *c;
+  }
+  else {
+    *x = 0.;
+    *y = 0.;
+    *c = 1.;
+    *s = 0.;
+  }
+  *x = fabs(*x * *y);
+}
+
+// restart: r = rhs - A x was computed with its partial norms
+__global__ void k_gm_restart(GmState *S, const double *__restrict__ part, int m)
+{
+  if(!S->active) return;
+  double rr = 0.;
+  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) rr += part[i];
+  rr = block_sum<double, 256>(rr);
+  if(threadIdx.x) return;
+  S->its += 1;
+  double alpha = sqrt(rr);
+  if(S->first) {
+    S->tol = S->rtol * alpha + 0.0;
+    S->res0 = alpha;
+    S->first = 0;
+  }
+  S->res = alpha;
+  S->g[0] = alpha;
+  S->k = 0;
+  S->did_cycle = 0;
+  S->breakdown = 0;
+  if(!(alpha > S->tol)) {  // converged (also for a zero right-hand side)
+    S->status = (alpha == alpha) ? 0 : -10;
+    S->res6 = alpha;
+    S->active = 0;
+    S->cycle = 0;
+    return;
+  }
+  S->scale = 1. / alpha;
+  S->cycle = 1;
+}
+
+// y = s * x, guarded by the cycle flag
+__global__ void k_gm_scale(int n, const GmState *__restrict__ S,
+                           const double *__restrict__ x, double *__restrict__ y)
+{
+  if(!S->cycle) return;
+  double s = S->scale;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x)
+    y[i] = s * x[i];
+}
+
+// partial dots <V_j, w>, j < k, over a fixed grid; part[j * B + block]
+__global__ void __launch_bounds__(256)
+k_gm_dots(int n, int k, const double *__restrict__ V, size_t ldv,
+          const double *__restrict__ w, double *__restrict__ part,
+          const GmState *__restrict__ S)
+{
+  if(!S->cycle) return;
+  for(int j0 = 0; j0 < k; j0 += 8) {
+    double acc[8];
+#pragma unroll
+    for(int u = 0; u < 8; u++) acc[u] = 0.;
+    for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+        i += (long long)gridDim.x * blockDim.x) {
+      double wi = w[i];
+#pragma unroll
+      for(int u = 0; u < 8; u++)
+        if(j0 + u < k) acc[u] += V[(size_t)(j0 + u) * ldv + i] * wi;
+    }
+#pragma unroll
+    for(int u = 0; u < 8; u++) {
+      if(j0 + u >= k) break;
+      double s = block_sum<double, 256>(acc[u]);
+      if(threadIdx.x == 0) part[(size_t)(j0 + u) * kReduceBlocks + blockIdx.x] = s;
+    }
+  }
+}
+
+// h[j] = sum of partials (one warp per j); pass 0 stores, pass 1 adds
+__global__ void k_gm_reduce(int k, const double *__restrict__ part, GmState *S,
+                            int pass)
+{
+  if(!S->cycle) return;
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for(int j = w; j < k; j += blockDim.x / 32) {
+    double v = 0.;
+    for(int b = lane; b < kReduceBlocks; b += 32)
+      v += part[(size_t)j * kReduceBlocks + b];
+    v = warp_sum(v);
+    if(lane == 0) {
+      if(pass == 0)
+        S->h1[j] = v;
+      else {
+        S->h2[j] = v;
+        S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = S->h1[j] + v;
+      }
+    }
+  }
+}
+
+// w -= sum_j h_j V_j (h from pass `pass`); with NORM the partial ||w||^2
+template <int NORM>
+__global__ void __launch_bounds__(256)
+k_gm_update(int n, int k, const double *__restrict__ V, size_t ldv,
+            double *__restrict__ w, double *__restrict__ part,
+            const GmState *__restrict__ S, int pass)
+{
+  if(!S->cycle) return;
+  __shared__ double h[kMaxKrylov];
+  for(int j = threadIdx.x; j < k; j += blockDim.x)
+    h[j] = pass == 0 ? S->h1[j] : S->h2[j];
+  __syncthreads();
+  double v = 0.;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x) {
+    double wi = w[i];
+    for(int j = 0; j < k; j++) wi -= h[j] * V[(size_t)j * ldv + i];
+    w[i] = wi;
+    v += wi * wi;
+  }
+  if(NORM) {
+    double s = block_sum<double, 256>(v);
+    if(threadIdx.x == 0) part[blockIdx.x] = s;
+  }
+}
+
+// end of one Arnoldi step: h(k+1,k), Givens rotations, stopping test
+__global__ void k_gm_step(int k, int m, GmState *S, const double *__restrict__ part)
+{
+  if(!S->cycle) return;
+  double rr = 0.;
+  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) rr += part[i];
+  rr = block_sum<double, 256>(rr);
+  if(threadIdx.x) return;
+  S->its += 1;
+  double *Hc = S->H + (size_t)(k - 1) * (kMaxKrylov + 1);  // column k
+  double nrm = sqrt(rr);
+  Hc[k] = nrm;
+  S->k = k;
+  S->did_cycle = 1;
+  if(!(nrm > 0.)) {  // mgsro ierr -3: the new vector depends on the others
+    S->breakdown = -3;
+    S->cycle = 0;
+    return;
+  }
+  // previous rotations on the new column, then a new one
+  for(int i = 0; i < k - 1; i++) {
+    double a = Hc[i], c = S->cs[i], s = S->sn[i];
+    Hc[i] = c * a + s * Hc[i + 1];
+    Hc[i + 1] = c * Hc[i + 1] - s * a;
+  }
+  double c, s;
+  givens_dev(&Hc[k - 1], &Hc[k], &c, &s);
+  S->cs[k - 1] = c;
+  S->sn[k - 1] = s;
+  double alpha = -s * S->g[k - 1];
+  S->g[k - 1] = c * S->g[k - 1];
+  S->g[k] = alpha;
+  alpha = fabs(alpha);
+  S->res = alpha;
+  S->scale = 1. / nrm;
+  if(!(k < m && !(alpha <= S->tol) && (S->maxit <= 0 || S->its < S->maxit)))
+    S->cycle = 0;  // end of this cycle after the scaling below is skipped
+}
+
+// scale the new basis vector (runs only while the cycle continues)
+__global__ void k_gm_scale_next(int n, const GmState *__restrict__ S,
+                                double *__restrict__ w, int k)
+{
+  if(!S->cycle || S->k != k) return;
+  double s = S->scale;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x)
+    w[i] *= s;
+}
+
+// end of a cycle: solve H y = g (upper triangular, k x k) on one thread
+__global__ void k_gm_solve_small(GmState *S)
+{
+  if(!S->active || !S->did_cycle || threadIdx.x) return;
+  int k = S->k;
+  const int ld = kMaxKrylov + 1;
+  while(k > 0 && S->H[(size_t)(k - 1) * ld + (k - 1)] == 0.) k--;  // iters.f:2141-2155
+  if(k == 0) {
+    S->status = -3;
+    S->breakdown = -4;
+    S->active = 0;
+    S->did_cycle = 0;
+    return;
+  }
+  S->k = k;
+  for(int i = k - 1; i >= 0; i--) {
+    double t = S->g[i];
+    for(int j = i + 1; j < k; j++) t -= S->H[(size_t)j * ld + i] * S->y[j];
+    S->y[i] = t / S->H[(size_t)i * ld + i];
+  }
+}
+
+// u = sum_j y_j Vj (GMRES) or x += sum_j y_j Z_j (FGMRES, ADD = 1)
+template <int ADD>
+__global__ void __launch_bounds__(256)
+k_gm_combine(int n, const double *__restrict__ V, size_t ldv,
+             double *__restrict__ out, const GmState *__restrict__ S)
+{
+  if(!S->active || !S->did_cycle) return;
+  __shared__ double y[kMaxKrylov];
+  int k = S->k;
+  for(int j = threadIdx.x; j < k; j += blockDim.x) y[j] = S->y[j];
+  __syncthreads();
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x) {
+    double s = ADD ? out[i] : 0.;
+    for(int j = 0; j < k; j++) s += y[j] * V[(size_t)j * ldv + i];
+    out[i] = s;
+  }
+}
+
+__global__ void k_gm_addto(int n, const double *__restrict__ u,
+                           double *__restrict__ x, const GmState *__restrict__ S)
+{
+  if(!S->active || !S->did_cycle) return;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x)
+    x[i] += u[i];
+}
+
+// after the update: the restart decision of iters.f:2196-2218
+__global__ void k_gm_after(GmState *S)
+{
+  if(!S->active || threadIdx.x) return;
+  S->res6 = S->res;
+  if(S->breakdown != 0) {
+    S->status = -3;
+    S->active = 0;
+    return;
+  }
+  bool more = (S->its < S->maxit || S->maxit <= 0) && (S->res6 > S->tol);
+  if(!more) {
+    if(S->res6 <= S->tol)
+      S->status = 0;
+    else if(S->its >= S->maxit && S->maxit > 0)
+      S->status = -1;
+    else
+      S->status = -10;
+    S->active = 0;
+  }
+}
+
+// flag pointer for the preconditioner inside a cycle: S->cycle
+static const int *cycle_flag(GmState *S) { return &S->cycle; }
+
+__global__ void k_gm_apply_ok(GmState *S, int *ok)
+{
+  // the update's preconditioner runs when a solution update is due
+  if(threadIdx.x == 0) *ok = (S->active && S->did_cycle) ? 1 : 0;
+}
+
+int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
+                double *x, const gb300_solver_params *p, gb300_solve_info *info,
+                Work &W)
+{
+  cudaStream_t st = A->ctx->stream;
+  int n = A->n;
+  bool flexible = (p->algorithm == 9);
+  if(p->algorithm != 8 && p->algorithm != 9) {
+    set_error("Algorithm %d with Preconditioner %d is not supported", p->algorithm,
+              p->preconditioner);
+    return GB300_ERR_UNSUPPORTED;
+  }
+  int m = p->krylov_size <= 1 ? 15 : p->krylov_size;
+  if(m > kMaxKrylov) {
+    set_error("Krylov_Size %d exceeds this backend's maximum %d", m, kMaxKrylov);
+    return GB300_ERR_UNSUPPORTED;
+  }
+  bool precond = (p->preconditioner == 6);
+  if(p->preconditioner != 0 && p->preconditioner != 6 && p->preconditioner != 8) {
+    set_error("Preconditioner %d is not supported by this backend", p->preconditioner);
+    return GB300_ERR_UNSUPPORTED;
+  }
+  bool fp32 = (p->precision != 0);
+  if(precond) {
+    int zr = 0;
+    // the factor is on A's values as given to the solver (scaled if needed)
+    GB_TRY(ilu_factor(A, val, fp32, &zr));
+    if(zr) {
+      info->status = zr;
+      set_error("Zero pivot on line %d in ILU", zr);
+      return GB300_ERR_ZERO_PIVOT;
+    }
+  }
+  size_t ldv = (size_t)n;
+  double *V = (double *)W.vec(0, sizeof(double) * ldv * (m + 1));
+  double *Z = flexible ? (double *)W.vec(1, sizeof(double) * ldv * m) : nullptr;
+  double *r = (double *)W.vec(2, sizeof(double) * n);
+  double *u = (double *)W.vec(3, sizeof(double) * n);
+  double *zt = (double *)W.vec(4, sizeof(double) * n);
+  float *t32 = fp32 ? (float *)W.vec(5, sizeof(float) * n) : nullptr;
+  double *part = (double *)W.vec(6, sizeof(double) * kReduceBlocks * (m + 1));
+  GmState *S = (GmState *)W.state(sizeof(GmState));
+  int *okflag = (int *)W.vec(7, sizeof(int));
+  if(!V || (flexible && !Z) || !r || !u || !zt || (fp32 && !t32) || !part || !S)
+    return GB300_ERR_CUDA;
+  GmState h0;
+  memset(&h0, 0, sizeof(h0));
+  h0.active = 1;
+  h0.first = 1;
+  h0.maxit = p->nb_iter_max;
+  h0.rtol = p->stopping_test;
+  h0.status = 1;
+  GB_CUDA(cudaMemcpyAsync(S, &h0, sizeof(GmState), cudaMemcpyHostToDevice, st));
+  GB_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));  // sol = 0
+
+  int gs = grid_for(n, 256, kReduceBlocks * 4);
+  auto precond_apply = [&](const double *v, double *z, const int *flag) {
+    if(precond)
+      ilu_apply(A, fp32, v, z, t32, flag, st);
+    else
+      k_cvt<double, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, z, flag);
+  };
+
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+  GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  // restart: r = rhs - A x, its norm, v1 = r / ||r||
+  residual64(A, val, x, rhs, r, part, st);
+  k_gm_restart<<<1, 256, 0, st>>>(S, part, m);
+  k_gm_scale<<<gs, 256, 0, st>>>(n, S, r, V);
+  for(int k = 1; k <= m; k++) {
+    double *vk = V + (size_t)(k - 1) * ldv;
+    double *w = V + (size_t)k * ldv;
+    double *z = flexible ? Z + (size_t)(k - 1) * ldv : zt;
+    precond_apply(vk, z, cycle_flag(S));
+    spmv_guarded(A, val, z, w, &S->cycle, st);
+    k_gm_dots<<<kReduceBlocks, 256, 0, st>>>(n, k, V, ldv, w, part, S);
+    k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 0);
+    k_gm_update<0><<<kReduceBlocks, 256, 0, st>>>(n, k, V, ldv, w, part, S, 0);
+    k_gm_dots<<<kReduceBlocks, 256, 0, st>>>(n, k, V, ldv, w, part, S);
+    k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 1);
+    k_gm_update<1><<<kReduceBlocks, 256, 0, st>>>(n, k, V, ldv, w, part, S, 1);
+    k_gm_step<<<1, 256, 0, st>>>(k, m, S, part);
+    k_gm_scale_next<<<gs, 256, 0, st>>>(n, S, w, k);
+  }
+  k_gm_solve_small<<<1, 32, 0, st>>>(S);
+  if(flexible)
+    k_gm_combine<1><<<gs, 256, 0, st>>>(n, Z, ldv, x, S);
+  else {
+    k_gm_combine<0><<<gs, 256, 0, st>>>(n, V, ldv, u, S);
+    k_gm_apply_ok<<<1, 32, 0, st>>>(S, okflag);
+    precond_apply(u, zt, okflag);
+    k_gm_addto<<<gs, 256, 0, st>>>(n, zt, x, S);
+  }
+  k_gm_after<<<1, 32, 0, st>>>(S);
+  GB_CUDA(cudaStreamEndCapture(st, &graph));
+  GB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+
+  int active = 1, launches = 0;
+  int max_launches = p->nb_iter_max > 0 ? p->nb_iter_max + 2 : 1 << 30;
+  while(active && launches < max_launches) {
+    GB_CUDA(cudaGraphLaunch(exec, st));
+    launches++;
+    GB_CUDA(cudaMemcpyAsync(&active, &S->active, sizeof(int),
+                            cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  GB_CUDA(cudaMemcpyAsync(&h0, S, sizeof(GmState), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  info->status = active ? -1 : h0.status;
+  info->iterations = h0.its;
+  info->residual_estimate = h0.res6;
+  return GB300_OK;
+}
+
+}  // namespace gb

@@ -1,0 +1,730 @@
+// Solve[A] on the GPU: the work of solve_matrix
+// (contrib/Sparskit/Sparskit.cpp:108-634) with the Krylov methods of
+// contrib/Sparskit/iters.f.
+//
+// Every scalar of a Krylov iteration (dot products, step lengths, the
+// stopping test of stopbis, iters.f:3275-3331) lives in device memory and is
+// computed by one-block control kernels, so iterations run back to back
+// without host round trips.  A fixed batch of iterations is captured once
+// in a CUDA graph and replayed; kernels after convergence see the device
+// flag `active == 0` and return at once.  The host reads one status word
+// per graph launch.
+//
+// Dot products use fixed-size partial-sum grids summed in a fixed order, so
+// a solve is bit-reproducible run to run.
+#include "krylov.cuh"
+
+namespace gb {
+
+// ---------------------------------------------------------------------------
+// scaling (scale_matrix DIAG_SCALING, Sparskit.cpp:978-1001: rowscal =
+// colscal = 1/sqrt(|a_ii|), A <- D A D applied as (a*s_i)*s_j, b <- D b,
+// x <- D y at the end)
+// ---------------------------------------------------------------------------
+__global__ void k_diag_scal(int n, const int *__restrict__ rowptr,
+                            const int *__restrict__ col,
+                            const double *__restrict__ val,
+                            double *__restrict__ s, int *__restrict__ zero)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= n) return;
+  double d = 0.;
+  for(int k = rowptr[i]; k < rowptr[i + 1]; k++)
+    if(col[k] == i) {
+      d = val[k];
+      break;
+    }
+  if(d != 0.)
+    s[i] = 1. / sqrt(fabs(d));
+  else {
+    s[i] = 1.;
+    atomicExch(zero, 1);
+  }
+}
+
+__global__ void k_scale_vals(int n, const int *__restrict__ rowptr,
+                             const int *__restrict__ col,
+                             const double *__restrict__ val,
+                             const double *__restrict__ s,
+                             double *__restrict__ out)
+{
+  int i = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if(i >= n) return;
+  double si = s[i];
+  for(int k = rowptr[i] + (threadIdx.x & 31); k < rowptr[i + 1]; k += 32)
+    out[k] = (val[k] * si) * s[col[k]];
+}
+
+__global__ void k_mul(int n, const double *a, const double *s, double *out)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i < n) out[i] = a[i] * s[i];
+}
+
+template <typename TO, typename TI>
+__global__ void k_convert(long long n, const TI *__restrict__ in,
+                          TO *__restrict__ out)
+{
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if(i < n) out[i] = (TO)in[i];
+}
+
+// ---------------------------------------------------------------------------
+// CG (iters.f:379-564, no preconditioner: Ml = Mr = I)
+// ---------------------------------------------------------------------------
+struct CgState {
+  double rho;    // <r, r> of the previous step (fpar(7))
+  double alpha;  // step length
+  double beta;
+  double tol;    // fpar(4) = rtol * ||r0|| + atol
+  double res;    // fpar(5) = fpar(6) = ||r||
+  double res0;   // fpar(3)
+  int active;
+  int status;    // ipar(1) at exit
+  int its;       // ipar(7)
+  int maxit;     // ipar(6)
+  // mixed precision (reliable updates)
+  double maxrr;  // largest FP32 ||r||^2 since the last update
+  double delta2; // update when ||r32||^2 < delta2 * maxrr
+  int update;    // this iteration replaces the residual in FP64
+  int convert;   // r32 <- r64 pending
+  int final_;    // the iteration cap was reached: last update then stop
+  int updates;   // residual replacements done
+};
+
+__global__ void k_cg_start(CgState *S, const double *__restrict__ part_rr,
+                           double rtol, int maxit)
+{
+  double rr = 0.;
+  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) rr += part_rr[i];
+  rr = block_sum<double, 256>(rr);
+  if(threadIdx.x == 0) {
+    S->rho = rr;
+    S->res0 = sqrt(rr);
+    S->res = S->res0;
+    S->tol = rtol * S->res0 + 0.0;
+    S->its = 1;  // the initial residual's matrix-vector product
+    S->maxit = maxit;
+    S->status = 1;
+    S->active = 1;
+    S->alpha = S->beta = 0.;
+    if(!(rr > 0.)) {  // zero right-hand side: x = 0 solves it
+      S->active = 0;
+      S->status = 0;
+    }
+  }
+}
+
+__global__ void k_cg_alpha(CgState *S, const double *__restrict__ part_pq)
+{
+  if(!S->active) return;
+  double pq = 0.;
+  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) pq += part_pq[i];
+  pq = block_sum<double, 256>(pq);
+  if(threadIdx.x == 0) {
+    S->its += 1;
+    // brkdn (iters.f:3368-3402)
+    bool bad = false;
+    if(pq > 0.) {
+      double b = 1. / pq;
+      if(!(b > 0.)) { bad = true; S->status = -9; }
+    }
+    else if(pq < 0.) {
+      double b = 1. / pq;
+      if(!(b < 0.)) { bad = true; S->status = -9; }
+    }
+    else if(pq == 0.) { bad = true; S->status = -3; }
+    else { bad = true; S->status = -9; }
+    if(bad) {
+      S->active = 0;
+      S->alpha = 0.;
+    }
+    else
+      S->alpha = S->rho / pq;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_cg_update(int n, const CgState *__restrict__ S, T *__restrict__ x,
+            T *__restrict__ r, const T *__restrict__ p, const T *__restrict__ q,
+            double *__restrict__ part)
+{
+  if(!S->active) return;
+  T a = (T)S->alpha;
+  double v = 0.;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x) {
+    x[i] += a * p[i];
+    T ri = r[i] - a * q[i];
+    r[i] = ri;
+    v += (double)ri * (double)ri;
+  }
+  double s = block_sum<double, 256>(v);
+  if(threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void k_cg_check(CgState *S, const double *__restrict__ part_rr)
+{
+  if(!S->active) return;
+  double rr = 0.;
+  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) rr += part_rr[i];
+  rr = block_sum<double, 256>(rr);
+  if(threadIdx.x == 0) {
+    // stopbis: the iteration cap first, then the residual test
+    if(S->maxit > 0 && S->its >= S->maxit) {
+      S->status = -1;
+      S->active = 0;
+      S->res = sqrt(rr);
+      return;
+    }
+    S->res = sqrt(rr);
+    if(!(S->res > S->tol)) {
+      S->status = (S->res == S->res) ? 0 : -10;
+      S->active = 0;
+      return;
+    }
+    S->beta = S->res * S->res / S->rho;
+    S->rho = S->res * S->res;
+  }
+}
+
+template <typename T>
+__global__ void k_cg_p(int n, const CgState *__restrict__ S, T *__restrict__ p,
+                       const T *__restrict__ r)
+{
+  if(!S->active) return;
+  T b = (T)S->beta;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x)
+    p[i] = r[i] + b * p[i];
+}
+
+template <typename T>
+__global__ void k_copy(long long n, const T *__restrict__ a, T *__restrict__ b)
+{
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if(i < n) b[i] = a[i];
+}
+
+// SpMV with the CG dot fused, guarded by the active flag
+template <int TPR, typename V, typename XT>
+__global__ void __launch_bounds__(256)
+k_cg_spmv(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
+          const V *__restrict__ val, const XT *__restrict__ p,
+          XT *__restrict__ q, double *__restrict__ part,
+          const CgState *__restrict__ S)
+{
+  if(!S->active) return;
+  const int rows_per_block = 256 / TPR;
+  int lane = threadIdx.x % TPR;
+  int sub = threadIdx.x / TPR;
+  double red = 0.0;
+  for(long long rb = (long long)blockIdx.x * rows_per_block; rb < n;
+      rb += (long long)gridDim.x * rows_per_block) {
+    long long row = rb + sub;
+    XT sum = 0;
+    if(row < n) {
+      int s = rowptr[row], e = rowptr[row + 1];
+      for(int k = s + lane; k < e; k += TPR)
+        sum += (XT)ld_stream(val + k) * p[ld_stream(col + k)];
+    }
+#pragma unroll
+    for(int o = TPR / 2; o > 0; o >>= 1)
+      sum += __shfl_down_sync(0xffffffffu, sum, o, TPR);
+    if(lane == 0 && row < n) {
+      q[row] = sum;
+      red += (double)p[row] * (double)sum;
+    }
+  }
+  double s = block_sum<double, 256>(red);
+  if(threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+template <typename V, typename XT>
+static void cg_spmv(const gb300_matrix *A, const V *val, const XT *p, XT *q,
+                    double *part, const CgState *S, cudaStream_t st)
+{
+  int n = A->n;
+  switch(A->tpr) {
+  case 4: k_cg_spmv<4><<<kReduceBlocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, p, q, part, S); break;
+  case 8: k_cg_spmv<8><<<kReduceBlocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, p, q, part, S); break;
+  case 16: k_cg_spmv<16><<<kReduceBlocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, p, q, part, S); break;
+  default: k_cg_spmv<32><<<kReduceBlocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, p, q, part, S); break;
+  }
+}
+
+// Runs CG on (A with values `val`) y = rhs, starting from y = 0, to
+// ||r|| <= rtol ||rhs||.  T is the vector type (double, or float with
+// float values).  Returns the final state in *hs.
+template <typename V, typename T>
+static int cg_run(const gb300_matrix *A, const V *val, const T *rhs, T *y,
+                  double rtol, int maxit, CgState *hs, Work &W)
+{
+  cudaStream_t st = A->ctx->stream;
+  int n = A->n;
+  T *r = (T *)W.vec(0, n * sizeof(T));
+  T *p = (T *)W.vec(1, n * sizeof(T));
+  T *q = (T *)W.vec(2, n * sizeof(T));
+  if(!r || !p || !q) return GB300_ERR_CUDA;
+  CgState *S = (CgState *)W.state(sizeof(CgState));
+  double *part = W.part();
+  if(!S || !part) return GB300_ERR_CUDA;
+  int gl = grid_for(n, 256);
+  // x0 = 0 (Sparskit.cpp:226); r = rhs - A*0 = rhs, p = r
+  GB_CUDA(cudaMemsetAsync(y, 0, n * sizeof(T), st));
+  k_copy<T><<<gl, 256, 0, st>>>(n, rhs, r);
+  k_copy<T><<<gl, 256, 0, st>>>(n, rhs, p);
+  if(sizeof(T) == 8)
+    dot_part64(n, (const double *)r, (const double *)r, part, st);
+  else
+    dot_part32(n, (const float *)r, (const float *)r, part, st);
+  k_cg_start<<<1, 256, 0, st>>>(S, part, rtol, maxit);
+  GB_CUDA(cudaGetLastError());
+
+  // capture a batch of iterations once
+  const int batch = n > 200000 ? 16 : 32;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+  GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  for(int it = 0; it < batch; it++) {
+    cg_spmv<V, T>(A, val, p, q, part, S, st);
+    k_cg_alpha<<<1, 256, 0, st>>>(S, part);
+    k_cg_update<T><<<kReduceBlocks, 256, 0, st>>>(n, S, y, r, p, q, part);
+    k_cg_check<<<1, 256, 0, st>>>(S, part);
+    k_cg_p<T><<<grid_for(n, 256, kReduceBlocks * 4), 256, 0, st>>>(n, S, p, r);
+  }
+  GB_CUDA(cudaStreamEndCapture(st, &graph));
+  GB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  int active = 1;
+  int launches = 0;
+  int max_launches = (maxit > 0 ? maxit / batch + 2 : 1 << 30);
+  while(active && launches < max_launches) {
+    GB_CUDA(cudaGraphLaunch(exec, st));
+    launches++;
+    GB_CUDA(cudaMemcpyAsync(&active, &S->active, sizeof(int),
+                            cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  GB_CUDA(cudaMemcpyAsync(hs, S, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  return GB300_OK;
+}
+
+// timed launches of the CG SpMV kernel (used for the roofline figure)
+int bench_spmv(gb300_matrix *A, int precision, int reps, double *ms)
+{
+  cudaStream_t st = A->ctx->stream;
+  int n = A->n;
+  Work W;
+  CgState h;
+  memset(&h, 0, sizeof(h));
+  h.active = 1;
+  CgState *S = (CgState *)W.state(sizeof(CgState));
+  double *part = W.part();
+  if(!S || !part) return GB300_ERR_CUDA;
+  GB_CUDA(cudaMemcpyAsync(S, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  cudaEvent_t e0, e1;
+  GB_CUDA(cudaEventCreate(&e0));
+  GB_CUDA(cudaEventCreate(&e1));
+  float t = 0.f;
+  if(precision == 0) {
+    double *p = (double *)W.vec(0, sizeof(double) * n);
+    double *q = (double *)W.vec(1, sizeof(double) * n);
+    if(!p || !q) return GB300_ERR_CUDA;
+    k_copy<double><<<grid_for(n, 256), 256, 0, st>>>(n, A->val.p, p);  // any data
+    for(int i = 0; i < 3; i++) cg_spmv<double, double>(A, A->val.p, p, q, part, S, st);
+    GB_CUDA(cudaEventRecord(e0, st));
+    for(int i = 0; i < reps; i++) cg_spmv<double, double>(A, A->val.p, p, q, part, S, st);
+    GB_CUDA(cudaEventRecord(e1, st));
+  }
+  else {
+    DevBuf<float> v32;
+    GB_TRY(v32.alloc(A->nnz));
+    k_convert<float, double><<<grid_for(A->nnz, 256), 256, 0, st>>>(A->nnz, A->val.p, v32.p);
+    float *p = (float *)W.vec(0, sizeof(float) * n);
+    float *q = (float *)W.vec(1, sizeof(float) * n);
+    if(!p || !q) return GB300_ERR_CUDA;
+    k_convert<float, double><<<grid_for(n, 256), 256, 0, st>>>(n, A->val.p, p);
+    for(int i = 0; i < 3; i++) cg_spmv<float, float>(A, v32.p, p, q, part, S, st);
+    GB_CUDA(cudaEventRecord(e0, st));
+    for(int i = 0; i < reps; i++) cg_spmv<float, float>(A, v32.p, p, q, part, S, st);
+    GB_CUDA(cudaEventRecord(e1, st));
+  }
+  GB_CUDA(cudaEventSynchronize(e1));
+  GB_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = (double)t / (reps > 0 ? reps : 1);
+  return GB300_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision CG: FP32 matrix, vectors and SpMV, with FP64 reliable
+// updates.  The FP32 iterate accumulates a correction x32; whenever the FP32
+// residual has dropped by delta since the last update (or claims
+// convergence), the correction is folded into the FP64 solution, the true
+// residual b - A x is recomputed in FP64 and replaces the FP32 residual,
+// and the search direction is kept.  Convergence is only ever declared on
+// the FP64 residual.  This is iterative refinement whose inner solves share
+// one Krylov sequence, so the iteration count stays close to the FP64 one.
+// ---------------------------------------------------------------------------
+__global__ void k_rcg_start(CgState *S, const double *__restrict__ part_rr,
+                            double rtol, int maxit, double delta)
+{
+  double rr = 0.;
+  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) rr += part_rr[i];
+  rr = block_sum<double, 256>(rr);
+  if(threadIdx.x == 0) {
+    S->rho = rr;
+    S->res0 = sqrt(rr);
+    S->res = S->res0;
+    S->tol = rtol * S->res0;
+    S->its = 1;
+    S->maxit = maxit;
+    S->status = 1;
+    S->active = 1;
+    S->maxrr = rr;
+    S->delta2 = delta * delta;
+    S->update = S->convert = S->final_ = 0;
+    S->updates = 0;
+    if(!(rr > 0.)) {
+      S->active = 0;
+      S->status = 0;
+    }
+  }
+}
+
+__global__ void k_rcg_check(CgState *S, const double *__restrict__ part_rr)
+{
+  if(!S->active) return;
+  double rr = 0.;
+  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) rr += part_rr[i];
+  rr = block_sum<double, 256>(rr);
+  if(threadIdx.x == 0) {
+    S->convert = 0;
+    double tol2 = S->tol * S->tol;
+    bool cap = (S->maxit > 0 && S->its >= S->maxit);
+    if(cap || !(rr > tol2) || rr < S->delta2 * S->maxrr) {
+      S->update = 1;
+      S->final_ = cap ? 1 : 0;
+      S->res = sqrt(rr);
+      return;
+    }
+    S->update = 0;
+    if(rr > S->maxrr) S->maxrr = rr;
+    S->beta = rr / S->rho;
+    S->rho = rr;
+    S->res = sqrt(rr);
+  }
+}
+
+__global__ void k_rcg_fold(int n, const CgState *__restrict__ S,
+                           double *__restrict__ x, float *__restrict__ x32)
+{
+  if(!S->active || !S->update) return;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x) {
+    x[i] += (double)x32[i];
+    x32[i] = 0.f;
+  }
+}
+
+__global__ void k_rcg_after(CgState *S, const double *__restrict__ part_rr)
+{
+  if(!S->active || !S->update) return;
+  double rr = 0.;
+  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) rr += part_rr[i];
+  rr = block_sum<double, 256>(rr);
+  if(threadIdx.x == 0) {
+    S->updates += 1;
+    S->res = sqrt(rr);
+    S->update = 0;
+    if(!(S->res > S->tol)) {
+      S->status = (S->res == S->res) ? 0 : -10;
+      S->active = 0;
+      return;
+    }
+    if(S->final_) {
+      S->status = -1;
+      S->active = 0;
+      return;
+    }
+    S->beta = rr / S->rho;
+    S->rho = rr;
+    S->maxrr = rr;
+    S->convert = 1;
+  }
+}
+
+__global__ void k_rcg_convert(int n, const CgState *__restrict__ S,
+                              const double *__restrict__ r, float *__restrict__ r32)
+{
+  if(!S->active || !S->convert) return;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x)
+    r32[i] = (float)r[i];
+}
+
+__global__ void k_fold_all(int n, double *__restrict__ x, const float *__restrict__ x32)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i < n) x[i] += (double)x32[i];
+}
+
+static int cg_mixed(const gb300_matrix *A, const double *val, const double *rhs,
+                    double *x, double rtol, int maxit, CgState *hs, Work &W)
+{
+  cudaStream_t st = A->ctx->stream;
+  int n = A->n;
+  DevBuf<float> v32;
+  GB_TRY(v32.alloc(A->nnz > 0 ? A->nnz : 1));
+  k_convert<float, double><<<grid_for(A->nnz, 256), 256, 0, st>>>(A->nnz, val, v32.p);
+  float *r32 = (float *)W.vec(0, n * sizeof(float));
+  float *p32 = (float *)W.vec(1, n * sizeof(float));
+  float *q32 = (float *)W.vec(2, n * sizeof(float));
+  float *x32 = (float *)W.vec(3, n * sizeof(float));
+  double *r64 = (double *)W.vec(4, n * sizeof(double));
+  CgState *S = (CgState *)W.state(sizeof(CgState));
+  double *part = W.part();
+  if(!r32 || !p32 || !q32 || !x32 || !r64 || !S || !part) return GB300_ERR_CUDA;
+  int gl = grid_for(n, 256);
+  int gs = grid_for(n, 256, kReduceBlocks * 4);
+  GB_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), st));
+  GB_CUDA(cudaMemsetAsync(x32, 0, n * sizeof(float), st));
+  k_convert<float, double><<<gl, 256, 0, st>>>(n, rhs, r32);
+  k_copy<float><<<gl, 256, 0, st>>>(n, r32, p32);
+  dot_part64(n, rhs, rhs, part, st);
+  k_rcg_start<<<1, 256, 0, st>>>(S, part, rtol, maxit, 0.1);
+  GB_CUDA(cudaGetLastError());
+
+  const int batch = n > 200000 ? 16 : 32;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+  GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  for(int it = 0; it < batch; it++) {
+    cg_spmv<float, float>(A, v32.p, p32, q32, part, S, st);
+    k_cg_alpha<<<1, 256, 0, st>>>(S, part);
+    k_cg_update<float><<<kReduceBlocks, 256, 0, st>>>(n, S, x32, r32, p32, q32, part);
+    k_rcg_check<<<1, 256, 0, st>>>(S, part);
+    k_rcg_fold<<<gs, 256, 0, st>>>(n, S, x, x32);
+    residual64_guarded(A, val, x, rhs, r64, part, &S->update, st);
+    k_rcg_after<<<1, 256, 0, st>>>(S, part);
+    k_rcg_convert<<<gs, 256, 0, st>>>(n, S, r64, r32);
+    k_cg_p<float><<<gs, 256, 0, st>>>(n, S, p32, r32);
+  }
+  GB_CUDA(cudaStreamEndCapture(st, &graph));
+  GB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  int active = 1, launches = 0;
+  int max_launches = (maxit > 0 ? maxit / batch + 3 : 1 << 30);
+  while(active && launches < max_launches) {
+    GB_CUDA(cudaGraphLaunch(exec, st));
+    launches++;
+    GB_CUDA(cudaMemcpyAsync(&active, &S->active, sizeof(int),
+                            cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  // anything not folded yet (a break-down stop) joins the FP64 solution
+  k_fold_all<<<gl, 256, 0, st>>>(n, x, x32);
+  GB_CUDA(cudaMemcpyAsync(hs, S, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if(active) hs->status = -1;
+  return GB300_OK;
+}
+
+// ---------------------------------------------------------------------------
+// work space owned by a solve
+// ---------------------------------------------------------------------------
+void *Work::vec(int slot, size_t bytes)
+{
+  if(slot < 0 || slot >= kSlots) {
+    set_error("work slot %d out of range", slot);
+    return nullptr;
+  }
+  if(vecs[slot].alloc(bytes) != GB300_OK) return nullptr;
+  return vecs[slot].p;
+}
+void *Work::state(size_t bytes)
+{
+  if(st.alloc(bytes) != GB300_OK) return nullptr;
+  return st.p;
+}
+double *Work::part()
+{
+  if(parts.alloc(kReduceBlocks * 64) != GB300_OK) return nullptr;
+  return parts.p;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 residual ||b - A x|| (fused), used by the refinement loop and for
+// the reported true residual
+// ---------------------------------------------------------------------------
+int true_residual(const gb300_matrix *A, const double *val, const double *x,
+                  const double *b, double *r, double *res, Work &W)
+{
+  cudaStream_t st = A->ctx->stream;
+  double *part = W.part();
+  double *d_out = (double *)W.vec(kScratchScalar, sizeof(double) * 2);
+  residual64(A, val, x, b, r, part, st);
+  sum_partials(part, d_out, st);
+  double h = 0.;
+  GB_CUDA(cudaMemcpyAsync(&h, d_out, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  *res = sqrt(h);
+  return GB300_OK;
+}
+
+int norm2_dev(int n, const double *v, double *out, Work &W, cudaStream_t st)
+{
+  double *part = W.part();
+  double *d_out = (double *)W.vec(kScratchScalar, sizeof(double) * 2);
+  dot_part64(n, v, v, part, st);
+  sum_partials(part, d_out, st);
+  double h = 0.;
+  GB_CUDA(cudaMemcpyAsync(&h, d_out, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  *out = sqrt(h);
+  return GB300_OK;
+}
+
+__global__ void k_axpy_scaled(int n, double a, const float *__restrict__ d,
+                              double *__restrict__ x)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i < n) x[i] += a * (double)d[i];
+}
+
+__global__ void k_to32_scaled(int n, double s, const double *__restrict__ r,
+                              float *__restrict__ o)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i < n) o[i] = (float)(r[i] * s);
+}
+
+// ---------------------------------------------------------------------------
+// solve_matrix
+// ---------------------------------------------------------------------------
+int solve(gb300_matrix *A, const gb300_vector *bvec,
+          const gb300_solver_params *p, gb300_vector *xvec,
+          gb300_solve_info *info)
+{
+  gb300_solve_info dummy;
+  if(!info) info = &dummy;
+  memset(info, 0, sizeof(*info));
+  if(!A->csr_valid) {
+    set_error("matrix not assembled");
+    return GB300_ERR_ARG;
+  }
+  int n = A->n;
+  if(bvec->n != n || xvec->n != n) {
+    set_error("vector sizes do not match the matrix");
+    return GB300_ERR_ARG;
+  }
+  if(n == 0) return GB300_OK;  // "No equations in linear system"
+  cudaStream_t st = A->ctx->stream;
+  Work W;
+
+  // zero-row check (Sparskit.cpp:220-223)
+  {
+    std::vector<int> rp(n + 1);
+    GB_CUDA(cudaMemcpyAsync(rp.data(), A->rowptr.p, sizeof(int) * (n + 1),
+                            cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    for(int i = 0; i < n; i++)
+      if(rp[i + 1] - rp[i] <= 0) {
+        set_error("Zero row in matrix (row %d)", i + 1);
+        return GB300_ERR_ZERO_ROW;
+      }
+  }
+
+  // the system actually solved: scaled copies when Scaling = 1
+  const double *val = A->val.p;
+  const double *rhs = bvec->d.p;
+  DevBuf<double> sval, srhs, s;
+  bool scaled = false;
+  if(p->scaling == 1) {
+    DevBuf<int> zero;
+    GB_TRY(zero.alloc(1));
+    GB_TRY(s.alloc(n));
+    GB_CUDA(cudaMemsetAsync(zero.p, 0, sizeof(int), st));
+    k_diag_scal<<<grid_for(n, 256), 256, 0, st>>>(n, A->rowptr.p, A->col.p,
+                                                   A->val.p, s.p, zero.p);
+    int hz = 0;
+    GB_CUDA(cudaMemcpyAsync(&hz, zero.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if(!hz) {  // else "Diagonal scaling aborted because of zero diagonal"
+      GB_TRY(sval.alloc(A->nnz));
+      GB_TRY(srhs.alloc(n));
+      k_scale_vals<<<grid_for(n, 8), 256, 0, st>>>(n, A->rowptr.p, A->col.p,
+                                                    A->val.p, s.p, sval.p);
+      k_mul<<<grid_for(n, 256), 256, 0, st>>>(n, bvec->d.p, s.p, srhs.p);
+      val = sval.p;
+      rhs = srhs.p;
+      scaled = true;
+    }
+  }
+  else if(p->scaling != 0) {
+    set_error("Scaling %d is not supported by this backend", p->scaling);
+    return GB300_ERR_UNSUPPORTED;
+  }
+
+  double *x = xvec->d.p;
+  int rc = GB300_OK;
+  if(p->algorithm == 1 && p->preconditioner != 6) {
+    // CG; Preconditioner 0 and 8 (DIAGONAL stores alu = 1: the identity,
+    // Sparskit.cpp:338-354) both leave the operator unchanged
+    if(p->precision == 0) {
+      CgState hs;
+      GB_TRY(cg_run<double, double>(A, val, rhs, x, p->stopping_test,
+                                    p->nb_iter_max, &hs, W));
+      info->status = hs.status;
+      info->iterations = hs.its;
+      info->residual_estimate = hs.res;
+    }
+    else {
+      // FP32 CG with FP64 reliable updates (residual replacement)
+      CgState hs;
+      GB_TRY(cg_mixed(A, val, rhs, x, p->stopping_test, p->nb_iter_max, &hs, W));
+      info->status = hs.status;
+      info->iterations = hs.its;
+      info->inner_iterations = hs.its - 1;
+      info->refinement_steps = hs.updates;
+      info->residual_estimate = hs.res;
+    }
+  }
+  else if(p->algorithm == 8 || p->algorithm == 9 ||
+          (p->algorithm == 1 && p->preconditioner == 6)) {
+    rc = gmres_solve(A, val, rhs, x, p, info, W);
+    if(rc != GB300_OK) return rc;
+  }
+  else {
+    set_error("Algorithm %d is not supported by this backend", p->algorithm);
+    return GB300_ERR_UNSUPPORTED;
+  }
+
+  // the reported true residual, on the system solved
+  {
+    double *r = (double *)W.vec(kScratchRes, sizeof(double) * n);
+    double res = 0., bn = 0.;
+    GB_TRY(true_residual(A, val, x, rhs, r, &res, W));
+    GB_TRY(norm2_dev(n, rhs, &bn, W, st));
+    info->true_residual = res;
+    info->rhs_norm = bn;
+  }
+  if(scaled)  // x <- D y (scale_vector COLUMN, Sparskit.cpp:631-632)
+    k_mul<<<grid_for(n, 256), 256, 0, st>>>(n, x, s.p, x);
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(st));
+  if(info->status != 0) {
+    set_error("Iterative solver terminated (code = %d) after %d iterations",
+              info->status, info->iterations);
+    return GB300_ERR_SOLVER;
+  }
+  return rc;
+}
+
+}  // namespace gb

@@ -1,0 +1,46 @@
+// Declarations shared by the sparse, assembly and solver translation units.
+#pragma once
+
+#include "common.cuh"
+
+namespace gb {
+
+int exclusive_scan(const int *in, long long n, long long *out, long long *total,
+                   DevBuf<long long> &tmp, cudaStream_t st);
+void choose_tpr(gb300_matrix *A);
+int build_pattern_from_elements(gb300_matrix *A, int ne, int nloc,
+                                const int *d_edofs, const unsigned char *d_cflag,
+                                int complex_mode);
+int build_csr_from_coo(gb300_matrix *A, long long m, const int *d_r,
+                       const int *d_c, const double *d_v);
+
+void spmv64(const gb300_matrix *A, const double *x, double *y, cudaStream_t st);
+void spmv_plain(const gb300_matrix *A, const double *val, const double *x,
+                double *y, cudaStream_t st);
+void spmv_guarded(const gb300_matrix *A, const double *val, const double *x,
+                  double *y, const int *flag, cudaStream_t st);
+void residual64(const gb300_matrix *A, const double *val, const double *x,
+                const double *b, double *r, double *part, cudaStream_t st);
+void residual64_guarded(const gb300_matrix *A, const double *val,
+                        const double *x, const double *b, double *r,
+                        double *part, const int *flag, cudaStream_t st);
+void spmv_dot64(const gb300_matrix *A, const double *val, const double *p,
+                double *q, double *part, cudaStream_t st);
+void spmv_dot32(const gb300_matrix *A, const float *val, const float *p,
+                float *q, double *part, cudaStream_t st);
+void sum_partials(const double *part, double *out, cudaStream_t st);
+void dot_part64(int n, const double *x, const double *y, double *part,
+                cudaStream_t st);
+void dot_part32(int n, const float *x, const float *y, double *part,
+                cudaStream_t st);
+
+int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t);
+int generate_pattern(gb300_matrix *A, const gb300_term_batch *t);
+
+struct ilu_data;
+void ilu_free(ilu_data *d);
+
+int solve(gb300_matrix *A, const gb300_vector *b, const gb300_solver_params *p,
+          gb300_vector *x, gb300_solve_info *info);
+
+}  // namespace gb

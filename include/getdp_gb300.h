@@ -1,0 +1,232 @@
+/*
+ * getdp_gb300 — C ABI of the GB300 (sm_103a) backend for GetDP's
+ * Generate/Solve hot path.
+ *
+ * GetDP talks to its linear-algebra backend through the LinAlg_* functions
+ * of src/kernel/LinAlg.h:90-213 (implemented for Sparskit in
+ * src/kernel/LinAlg_SPARSKIT.cpp).  This library provides the device-side
+ * objects and operations behind a drop-in replacement of that file
+ * (getdp_gb300/getdp_backend/LinAlg_GB300.cpp) plus one batched entry point
+ * for the element loop of Treatment_FemFormulation
+ * (src/kernel/Treatment_Formulation.cpp:413-618), which per-entry
+ * LinAlg_AddDoubleInMatrix calls cannot carry to a GPU.
+ *
+ * Conventions: plain C types only; indices are 0-based as in GetDP's calls
+ * (DofData.cpp:1478-1486); every function returns GB300_OK or an error code
+ * and the message is available from gb300_last_error().  Nothing here
+ * aborts the process: device-side failures are reported as status codes.
+ */
+#ifndef GETDP_GB300_H
+#define GETDP_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB300_OK 0
+#define GB300_ERR_ARG 1          /* invalid argument */
+#define GB300_ERR_CUDA 2         /* CUDA runtime error (or no device) */
+#define GB300_ERR_UNSUPPORTED 3  /* option not implemented by this backend */
+#define GB300_ERR_SOLVER 4       /* Krylov solver did not converge (info) */
+#define GB300_ERR_ZERO_PIVOT 5   /* ILU(0) met a zero pivot (info.status) */
+#define GB300_ERR_CAPACITY 6     /* a row exceeds a fixed work capacity */
+#define GB300_ERR_ZERO_ROW 7     /* empty matrix row (Sparskit.cpp:220-223) */
+
+typedef struct gb300_ctx gb300_ctx;
+typedef struct gb300_vector gb300_vector;
+typedef struct gb300_matrix gb300_matrix;
+
+/* Message of the last error on the calling thread ("" if none). */
+const char *gb300_last_error(void);
+int gb300_version(void);
+
+/* ---- context: one device, one stream -------------------------------- */
+int gb300_ctx_create(int device, gb300_ctx **out);
+int gb300_ctx_destroy(gb300_ctx *ctx);
+int gb300_ctx_synchronize(gb300_ctx *ctx);
+/* page-locked host memory for fast host<->device copies */
+int gb300_host_alloc(size_t bytes, void **out);
+int gb300_host_free(void *p);
+/* raw device buffers (e.g. element tables kept resident between calls)
+   and copies on the context's stream (synchronous on return) */
+int gb300_device_alloc(gb300_ctx *ctx, size_t bytes, void **out);
+int gb300_device_free(gb300_ctx *ctx, void *p);
+int gb300_copy_to_device(gb300_ctx *ctx, void *dst, const void *src, size_t bytes);
+int gb300_copy_to_host(gb300_ctx *ctx, void *dst, const void *src, size_t bytes);
+
+/* ---- solver parameters --------------------------------------------- */
+/* The fields are the keys of Sparskit's solver.par, same meaning and
+   defaults (contrib/Sparskit/Sparskit.h:83-103 Solver_Params,
+   Sparskit.cpp:1847-1868 Tab_Params).  Codes: Algorithm 1 CG, 8 GMRES,
+   9 FGMRES; Preconditioner 0 none, 6 ILU0, 8 DIAGONAL; Scaling 0 none,
+   1 diagonal (D^-1/2 A D^-1/2).  The last three fields are extensions of
+   this backend (keys Sparskit would reject as unknown). */
+typedef struct gb300_solver_params {
+  int matrix_format;
+  int matrix_printing;
+  int matrix_storage;
+  int scaling;
+  int renumbering_technique;
+  int preconditioner;
+  int preconditioner_position;
+  int nb_fill;
+  double permutation_tolerance;
+  double dropping_tolerance;
+  double diagonal_compensation;
+  int re_use_ilu;
+  int algorithm;
+  int krylov_size;
+  double ic_acceleration;
+  int re_use_lu;
+  int iterative_improvement;
+  int nb_iter_max;
+  double stopping_test;
+  /* extensions */
+  int precision;          /* Precision: 0 FP64, 1 FP32 inner solves in FP64 refinement */
+  double inner_tolerance; /* Inner_Tolerance: relative reduction per inner solve */
+  int inner_iter_max;     /* Inner_Iter_Max */
+} gb300_solver_params;
+
+/* Replaces Sparskit's init_solver defaults (Sparskit.cpp:1847-1868). */
+void gb300_solver_params_default(gb300_solver_params *p);
+/* One "-Name value" override (init_solver_option, Sparskit.cpp:2016-2043):
+   GB300_ERR_ARG for an unknown name, like "Unknown solver parameter". */
+int gb300_solver_params_set(gb300_solver_params *p, const char *name,
+                            const char *value);
+/* Reads a solver.par file ("Name value" pairs and C comments,
+   init_solver Sparskit.cpp:1895-2013); unknown names are skipped. */
+int gb300_solver_params_read(gb300_solver_params *p, const char *path);
+
+typedef struct gb300_solve_info {
+  int status;            /* Sparskit ipar(1): 0 converged, -1 too many
+                            iterations, -3 break-down, -9/-10 abnormal
+                            numbers; for a zero pivot: its row (1-based) */
+  int iterations;        /* ipar(7): matrix-vector products counted as
+                            Sparskit counts them */
+  double residual_estimate; /* fpar(6) of the (last) Krylov solve */
+  double true_residual;  /* ||b - A x||_2 of the returned x, in FP64, on the
+                            system actually solved (scaled if Scaling=1) */
+  double rhs_norm;       /* ||b||_2 of that system */
+  int refinement_steps;  /* FP64 refinement steps (Precision 1) */
+  int inner_iterations;  /* FP32 inner iterations (Precision 1) */
+} gb300_solve_info;
+
+/* ---- vectors (device resident, FP64) -------------------------------- */
+/* LinAlg_CreateVector / DestroyVector / ZeroVector / SetVector /
+   GetDoubleInVector (LinAlg_SPARSKIT.cpp:115-127, :160, :285-300). */
+int gb300_vector_create(gb300_ctx *ctx, int n, gb300_vector **out);
+int gb300_vector_destroy(gb300_vector *v);
+int gb300_vector_zero(gb300_vector *v);
+int gb300_vector_set(gb300_vector *v, const double *host);
+int gb300_vector_get(const gb300_vector *v, double *host);
+int gb300_vector_size(const gb300_vector *v, int *n);
+/* LinAlg_VectorNorm2 (norm2_vector) */
+int gb300_vector_norm2(const gb300_vector *v, double *norm);
+/* LinAlg_AddScalarInVector / AddDoubleInVector for a batch of entries
+   (host arrays), added in order */
+int gb300_vector_add_values(gb300_vector *v, int count, const int *idx,
+                            const double *val);
+
+/* ---- matrices (device CSR, rows sorted by column) -------------------- */
+/* LinAlg_CreateMatrix / DestroyMatrix (LinAlg_SPARSKIT.cpp:121-134). */
+int gb300_matrix_create(gb300_ctx *ctx, int n, gb300_matrix **out);
+int gb300_matrix_destroy(gb300_matrix *A);
+/* Forget all entries (the Generate path's ZeroMatrix: destroy+create,
+   SolvingOperations.cpp:175-184). */
+int gb300_matrix_reset(gb300_matrix *A);
+/* LinAlg_ZeroMatrix (LinAlg_SPARSKIT.cpp:163-170): keep the pattern, zero
+   the values, and make sure every diagonal entry exists. */
+int gb300_matrix_zero(gb300_matrix *A);
+/* LinAlg_AddDoubleInMatrix (LinAlg_SPARSKIT.cpp:392-400): staged on the
+   host in call order; duplicates are summed in that order. */
+int gb300_matrix_add_double(gb300_matrix *A, double d, int i, int j);
+/* LinAlg_AddComplexInMatrix (LinAlg_SPARSKIT.cpp:402-413): the 2x2 real
+   block [[d1, -d2], [d2, d1]] at rows i,k and columns j,l; zero parts are
+   skipped exactly as the reference skips them. */
+int gb300_matrix_add_complex(gb300_matrix *A, double d1, double d2, int i,
+                             int j, int k, int l);
+/* Bulk form of add_double (host arrays). */
+int gb300_matrix_add_coo(gb300_matrix *A, long long count, const int *i,
+                         const int *j, const double *v);
+/* LinAlg_AssembleMatrix: merge the staged entries into the device CSR
+   (the csr_format step, Sparskit.cpp:2186-2217, done on the GPU). */
+int gb300_matrix_assemble(gb300_matrix *A);
+int gb300_matrix_size(const gb300_matrix *A, int *n);
+int gb300_matrix_nnz(const gb300_matrix *A, long long *nnz);
+/* copy the CSR to host arrays (rowptr n+1, col nnz, val nnz) */
+int gb300_matrix_get_csr(const gb300_matrix *A, int *rowptr, int *col,
+                         double *val);
+/* replace the matrix by a host CSR (sorted rows) */
+int gb300_matrix_set_csr(gb300_matrix *A, long long nnz, const int *rowptr,
+                         const int *col, const double *val);
+/* LinAlg_ProdMatrixVector (prod_matrix_vector, Sparskit.cpp:1080-1122) */
+int gb300_matrix_mult(gb300_matrix *A, const gb300_vector *x, gb300_vector *y);
+
+/* ---- the batched element loop (Generate) ---------------------------- */
+/* One canonical formulation = the Galerkin terms GetDP's element loop
+   would evaluate one element at a time (Cal_GalerkinTermOfFemEquation.cpp
+   :531-1014) for all elements at once. */
+#define GB300_TERM_TRI3_MAGNETOSTATIC 1
+/*   2D a_z, BF_PerpendicularEdge on 3-node triangles, 3-point Gauss:
+     [coef * Dof{d a}, {d a}] + [-source, {a}]; coef = nu, source = J_z */
+#define GB300_TERM_TRI3_EDDY_COMPLEX 2
+/*   as above with Type Complex (two harmonics, interleaved unknowns) plus
+     DtDof[coef2 * Dof{a}, {a}] (coef2 = sigma) times j*omega, omega = p0 */
+#define GB300_TERM_TET10_ELASTICITY 3
+/*   3D linear elasticity on 10-node tets, 4-point Gauss: the nine terms
+     [-C_ij * Dof{d u_j}, {d u_i}] (Lib_Elasticity_u.pro C tensors with
+     E = coef, Poisson = p0) + [f_z, {u_z}] with f_z = p1.  elem_dofs holds
+     30 entries per element: ux nodes 1..10, uy nodes, uz nodes */
+#define GB300_TERM_TET4_EDGE_CURLCURL 4
+/*   3D Whitney edges (BF_Edge) on 4-node tets, 4-point Gauss:
+     [coef * Dof{d a}, {d a}] + [p0 * coef * Dof{a}, {a}] + [-js, {a}],
+     js = p1 * (-(y-0.5), x-0.5, 0) / r in elements with source != 0 */
+
+typedef struct gb300_term_batch {
+  int kind;
+  int n_nodes;
+  int n_elems;
+  const double *nodes;           /* n_nodes x 3 */
+  const int *elems;              /* n_elems x vertices, 0-based */
+  const int *elem_dofs;          /* n_elems x local DOFs: unknown or -1 */
+  const signed char *elem_sign;  /* n_elems x local DOFs (edges) or NULL */
+  const double *coef;            /* per element */
+  const double *source;          /* per element, or NULL */
+  const double *coef2;           /* per element, or NULL */
+  double p0, p1, p2;
+  int on_device;                 /* 1: the arrays above are device pointers */
+} gb300_term_batch;
+
+/* Build the CSR pattern of A from the element tables (rows of unknowns
+   touched by each element, sorted, no duplicates: the pattern the
+   reference's linked lists end up with) and zero A and b. */
+int gb300_generate_pattern(gb300_matrix *A, const gb300_term_batch *t);
+/* Evaluate every element matrix and add it into A and b (A's pattern must
+   contain the element pairs: gb300_generate_pattern). */
+int gb300_generate_values(gb300_matrix *A, gb300_vector *b,
+                          const gb300_term_batch *t);
+
+/* ---- measurement ---------------------------------------------------- */
+/* CUDA events on the context's stream (slots 0..15), for timing calls
+   made through this library on the device. */
+int gb300_event_record(gb300_ctx *ctx, int slot);
+int gb300_event_elapsed(gb300_ctx *ctx, int slot0, int slot1, float *ms);
+/* Average device time of one launch of the solver's CSR SpMV kernel (the
+   CG form q = A p with <p, q> fused; precision 0 FP64, 1 FP32 values and
+   vectors) over `reps` launches timed with CUDA events after a warm-up. */
+int gb300_bench_spmv(gb300_matrix *A, int precision, int reps, double *ms);
+
+/* ---- solve ------------------------------------------------------------ */
+/* LinAlg_Solve -> solve_matrix (Sparskit.cpp:108-634) on the GPU.  A and b
+   are not modified (Sparskit scales them in place; here scaling acts on
+   private copies).  x receives the solution. */
+int gb300_solve(gb300_matrix *A, const gb300_vector *b,
+                const gb300_solver_params *p, gb300_vector *x,
+                gb300_solve_info *info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

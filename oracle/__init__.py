@@ -75,6 +75,23 @@ def _p(a, ct):
 
 def assemble(problem, dofmap, ilu: str = "64"):
     """Run the restated element loop; returns (indptr, indices, data, b)."""
+    rr, cc, vv, b = assemble_coo(problem, dofmap, ilu)
+    L = lib(ilu)
+    I32, D = ctypes.c_int32, ctypes.c_double
+    n = dofmap.n_dof
+    nz = len(vv)
+    indptr = np.empty(n + 1, np.int32)
+    indices = np.empty(max(nz, 1), np.int32)
+    data = np.empty(max(nz, 1), np.float64)
+    nnz = L.oracle_coo_to_csr(n, ctypes.c_int64(nz), _p(rr, I32), _p(cc, I32),
+                              _p(vv, D), _p(indptr, I32), _p(indices, I32),
+                              _p(data, D))
+    return indptr, indices[:nnz].copy(), data[:nnz].copy(), b
+
+
+def assemble_coo(problem, dofmap, ilu: str = "64"):
+    """The matrix contributions in the reference's call order (the
+    LinAlg_AddDoubleInMatrix sequence) and the RHS: (rows, cols, vals, b)."""
     L = lib(ilu)
     m = problem.mesh
     n = dofmap.n_dof
@@ -84,7 +101,9 @@ def assemble(problem, dofmap, ilu: str = "64"):
     edofs = np.ascontiguousarray(dofmap.elem_dofs, np.int32)
     nloc = edofs.shape[1]
     f = problem.formulation
-    cap = ne * nloc * nloc * (4 if f == "eddy2d" else 1) * 2
+    # per element: eddy 4 entries per pair (2 real + 2 imaginary), curl-curl
+    # two terms (curl and mass), the others one
+    cap = ne * nloc * nloc * {"eddy2d": 4, "curlcurl": 2}.get(f, 1)
     rr = np.empty(cap, np.int32)
     cc = np.empty(cap, np.int32)
     vv = np.empty(cap, np.float64)
@@ -120,13 +139,7 @@ def assemble(problem, dofmap, ilu: str = "64"):
         raise ValueError(f)
     if nz > cap:
         raise RuntimeError("oracle COO capacity exceeded")
-    indptr = np.empty(n + 1, np.int32)
-    indices = np.empty(nz, np.int32)
-    data = np.empty(nz, np.float64)
-    nnz = L.oracle_coo_to_csr(n, ctypes.c_int64(nz), _p(rr, I32), _p(cc, I32),
-                              _p(vv, D), _p(indptr, I32), _p(indices, I32),
-                              _p(data, D))
-    return indptr, indices[:nnz].copy(), data[:nnz].copy(), b
+    return rr[:nz].copy(), cc[:nz].copy(), vv[:nz].copy(), b
 
 
 def solve(indptr, indices, data, b, algorithm=GMRES, preconditioner=ILU0,

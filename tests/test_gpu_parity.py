@@ -1,0 +1,261 @@
+"""GPU parity: the CUDA path against the reference's outputs and the oracle.
+
+Tolerances (FP64):
+* CSR pattern: identical to the reference's (bit-exact integers);
+* matrix and RHS values: |gpu - ref| <= 1e-12 * |ref| + 1e-14 * max|row of ref|
+  (summation order differs: atomics, fused multiply-adds);
+* the LinAlg add path (entries added one by one in the reference's call
+  order): bit-exact;
+* solutions: converged (status 0); with the reference's own tolerance the
+  GPU solution is within 1e-6 relative of the oracle's and the iteration
+  counts agree within 5 % + 2; with Stopping_Test 1e-14 within 1e-10.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from getdp_gb300 import generate as G_
+from getdp_gb300 import linalg as LA
+from getdp_gb300 import workloads as W
+from tests import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+ASSEMBLY_CASES = [n for n in G.names() if not n.endswith("ilu32")]
+
+
+def close_values(got, ref, indptr):
+    rowmax = np.zeros(len(ref))
+    for i in range(len(indptr) - 1):
+        s, e = indptr[i], indptr[i + 1]
+        if e > s:
+            rowmax[s:e] = np.max(np.abs(ref[s:e]))
+    return np.all(np.abs(got - ref) <= 1e-12 * np.abs(ref) + 1e-14 * rowmax)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from getdp_gb300 import build
+    build.build()
+    oracle.build()
+
+
+@pytest.mark.parametrize("name", ASSEMBLY_CASES)
+def test_generate_matches_reference(name):
+    d, p, dm = G.load(name)
+    A, b = G_.generate_problem(p, dm)
+    ip, ix, dv = A.csr()
+    assert np.array_equal(ip, d["indptr"])
+    assert np.array_equal(ix, d["indices"])
+    assert close_values(dv, d["data"], d["indptr"])
+    bb = b.numpy()
+    assert np.all(np.abs(bb - d["b"]) <= 1e-12 * np.abs(d["b"]) +
+                  1e-14 * np.max(np.abs(d["b"])))
+
+
+@pytest.mark.parametrize("name", ASSEMBLY_CASES)
+def test_linalg_add_path_bit_exact(name):
+    # the reference's LinAlg_AddDoubleInMatrix sequence, entry by entry
+    d, p, dm = G.load(name)
+    rr, cc, vv, b = oracle.assemble_coo(p, dm)
+    A = LA.LinAlg_CreateMatrix(None, dm.n_dof)
+    A.add_coo(rr, cc, vv)
+    LA.LinAlg_AssembleMatrix(A)
+    ip, ix, dv = A.csr()
+    assert np.array_equal(ip, d["indptr"])
+    assert np.array_equal(ix, d["indices"])
+    # the same triplets merged by the oracle on this machine: bit-exact
+    oip, oix, odv, _ = oracle.assemble(p, dm)
+    assert np.array_equal(dv, odv), (
+        f"{np.sum(dv != odv)} entries differ, max rel "
+        f"{np.max(np.abs(dv - odv) / np.maximum(np.abs(odv), 1e-300)):.2e}")
+    # and the reference's values (an element value computed on another
+    # architecture can differ in its last bit)
+    assert close_values(dv, d["data"], d["indptr"])
+
+
+def _solver(params: dict):
+    S = LA.LinAlg_CreateSolver(None)
+    for k, v in params.items():
+        S.set(k, v)
+    return S
+
+
+def _golden_params(d):
+    return {str(k): (v if str(k) == "Stopping_Test" else int(v))
+            for k, v in zip(d["par_keys"], d["par_vals"])}
+
+
+@pytest.mark.parametrize("name", ASSEMBLY_CASES)
+def test_solve_matches_oracle(name):
+    d, p, dm = G.load(name)
+    par = _golden_params(d)
+    par["Renumbering_Technique"] = 0  # the GPU keeps GetDP's DOF order
+    A = LA.LinAlg_CreateMatrix(None, dm.n_dof)
+    A.set_csr(d["indptr"], d["indices"], d["data"])
+    b = LA.LinAlg_CreateVector(None, dm.n_dof)
+    b.set(d["b"])
+    x = LA.LinAlg_CreateVector(None, dm.n_dof)
+    info = LA.LinAlg_Solve(A, b, _solver(par), x)
+    kw = oracle.params_from_golden(d["par_keys"], d["par_vals"])
+    kw["renumbering"] = 0
+    kw["stopping_test"] = float(np.float32(kw["stopping_test"]))
+    xo, st, its, _ = oracle.solve(d["indptr"], d["indices"], d["data"], d["b"], **kw)
+    assert st == 0 and info["status"] == 0, (info, st)
+    assert abs(info["iterations"] - its) <= 0.05 * its + 2, (info["iterations"], its)
+    xg = x.numpy()
+    assert np.linalg.norm(xg - xo) <= 1e-6 * np.linalg.norm(xo)
+
+
+@pytest.mark.parametrize("name", ["ms2d_n24", "el_p2_n3", "cc_edge_n4", "eddy_n8"])
+def test_tight_solve_within_1e10(name):
+    d, p, dm = G.load(name)
+    par = _golden_params(d)
+    par.update(Renumbering_Technique=0, Stopping_Test="1e-14", Nb_Iter_Max=20000)
+    A = LA.LinAlg_CreateMatrix(None, dm.n_dof)
+    A.set_csr(d["indptr"], d["indices"], d["data"])
+    b = LA.LinAlg_CreateVector(None, dm.n_dof)
+    b.set(d["b"])
+    x = LA.LinAlg_CreateVector(None, dm.n_dof)
+    info = LA.LinAlg_Solve(A, b, _solver(par), x)
+    kw = oracle.params_from_golden(d["par_keys"], d["par_vals"])
+    kw.update(renumbering=0, stopping_test=float(np.float32(1e-14)), nb_iter_max=20000)
+    xo, st, its, _ = oracle.solve(d["indptr"], d["indices"], d["data"], d["b"], **kw)
+    assert info["status"] == 0 and st == 0, (info, st)
+    assert np.linalg.norm(x.numpy() - xo) <= 1e-10 * np.linalg.norm(xo)
+
+
+def test_mixed_precision_cg_reaches_1e8():
+    p = W.elasticity_p2(n=4, seed=3)
+    dm = W.dofmap_for(p)
+    A, b = G_.generate_problem(p, dm)
+    x = LA.LinAlg_CreateVector(None, dm.n_dof)
+    S = _solver({"Algorithm": 1, "Preconditioner": 0, "Scaling": 1,
+                 "Stopping_Test": "1e-8", "Nb_Iter_Max": 100000, "Precision": 1})
+    info = LA.LinAlg_Solve(A, b, S, x)
+    assert info["status"] == 0
+    assert info["true_residual"] <= 1e-8 * info["rhs_norm"] * 1.0000001
+    assert info["refinement_steps"] >= 1
+    # same answer as the FP64 solve
+    x64 = LA.LinAlg_CreateVector(None, dm.n_dof)
+    S64 = _solver({"Algorithm": 1, "Preconditioner": 0, "Scaling": 1,
+                   "Stopping_Test": "1e-8", "Nb_Iter_Max": 100000})
+    LA.LinAlg_Solve(A, b, S64, x64)
+    assert np.linalg.norm(x.numpy() - x64.numpy()) <= 1e-5 * np.linalg.norm(x64.numpy())
+
+
+def test_mixed_precision_fgmres_ilu32():
+    p = W.magnetostatics_2d(n=48, seed=7)
+    dm = W.dofmap_for(p)
+    A, b = G_.generate_problem(p, dm)
+    x = LA.LinAlg_CreateVector(None, dm.n_dof)
+    S = _solver({"Algorithm": 9, "Preconditioner": 6, "Krylov_Size": 50,
+                 "Renumbering_Technique": 0, "Stopping_Test": "1e-10",
+                 "Precision": 1})
+    info = LA.LinAlg_Solve(A, b, S, x)
+    assert info["status"] == 0
+    assert info["true_residual"] <= 2e-10 * info["rhs_norm"]
+
+
+def test_zero_rhs_gives_zero_solution():
+    d, p, dm = G.load("ms2d_n8")
+    A = LA.LinAlg_CreateMatrix(None, dm.n_dof)
+    A.set_csr(d["indptr"], d["indices"], d["data"])
+    b = LA.LinAlg_CreateVector(None, dm.n_dof)
+    x = LA.LinAlg_CreateVector(None, dm.n_dof)
+    x.set(np.ones(dm.n_dof))
+    info = LA.LinAlg_Solve(A, b, _solver({"Algorithm": 8, "Preconditioner": 6,
+                                          "Renumbering_Technique": 0}), x)
+    assert info["status"] == 0
+    assert not np.any(x.numpy())
+
+
+def test_zero_pivot_is_reported():
+    A = LA.LinAlg_CreateMatrix(None, 2)
+    A.set_csr([0, 2, 4], [0, 1, 0, 1], [0.0, 1.0, 1.0, 1.0])
+    b = LA.LinAlg_CreateVector(None, 2)
+    b.set(np.ones(2))
+    x = LA.LinAlg_CreateVector(None, 2)
+    with pytest.raises(LA.GetDPError) as e:
+        LA.LinAlg_Solve(A, b, _solver({"Algorithm": 8, "Preconditioner": 6,
+                                       "Renumbering_Technique": 0}), x)
+    assert e.value.code == 5 and "Zero pivot on line 1" in str(e.value)
+
+
+def test_zero_row_is_reported():
+    A = LA.LinAlg_CreateMatrix(None, 3)
+    A.set_csr([0, 1, 1, 2], [0, 2], [1.0, 1.0])
+    b = LA.LinAlg_CreateVector(None, 3)
+    x = LA.LinAlg_CreateVector(None, 3)
+    with pytest.raises(LA.GetDPError) as e:
+        LA.LinAlg_Solve(A, b, _solver({"Algorithm": 8}), x)
+    assert e.value.code == 7
+
+
+def test_iteration_cap_is_a_warning():
+    d, p, dm = G.load("el_p2_n3")
+    A = LA.LinAlg_CreateMatrix(None, dm.n_dof)
+    A.set_csr(d["indptr"], d["indices"], d["data"])
+    b = LA.LinAlg_CreateVector(None, dm.n_dof)
+    b.set(d["b"])
+    x = LA.LinAlg_CreateVector(None, dm.n_dof)
+    info = LA.LinAlg_Solve(A, b, _solver({"Algorithm": 1, "Preconditioner": 0,
+                                          "Scaling": 1, "Nb_Iter_Max": 10}), x)
+    assert info["status"] == -1 and info["iterations"] == 10 and "warning" in info
+
+
+def test_missing_pattern_entry_is_an_error():
+    p = W.magnetostatics_2d(n=4, seed=1)
+    dm = W.dofmap_for(p)
+    A = LA.LinAlg_CreateMatrix(None, dm.n_dof)
+    ident = np.arange(dm.n_dof + 1, dtype=np.int32)
+    A.set_csr(ident, np.arange(dm.n_dof, dtype=np.int32), np.ones(dm.n_dof))
+    b = LA.LinAlg_CreateVector(None, dm.n_dof)
+    arrays = G_.term_arrays(p, dm)
+    import ctypes
+    from getdp_gb300 import _lib
+    with pytest.raises(LA.GetDPError):
+        _lib.check(_lib.load().gb300_generate_values(
+            A.h, b.h, ctypes.byref(G_.host_batch(arrays))))
+
+
+def test_empty_system():
+    A = LA.LinAlg_CreateMatrix(None, 0)
+    A.set_csr([0], [], [])
+    b = LA.LinAlg_CreateVector(None, 0)
+    x = LA.LinAlg_CreateVector(None, 0)
+    info = LA.LinAlg_Solve(A, b, _solver({}), x)
+    assert info["status"] == 0
+
+
+def test_linalg_product_and_norm():
+    d, p, dm = G.load("cc_edge_n4")
+    A = LA.LinAlg_CreateMatrix(None, dm.n_dof)
+    A.set_csr(d["indptr"], d["indices"], d["data"])
+    v = LA.LinAlg_CreateVector(None, dm.n_dof)
+    rng = np.random.default_rng(0)
+    xv = rng.standard_normal(dm.n_dof)
+    v.set(xv)
+    y = LA.LinAlg_CreateVector(None, dm.n_dof)
+    LA.LinAlg_ProdMatrixVector(A, v, y)
+    import scipy.sparse as sp
+    ref = sp.csr_matrix((d["data"], d["indices"], d["indptr"])) @ xv
+    assert np.allclose(y.numpy(), ref, rtol=1e-13, atol=1e-13 * np.max(np.abs(ref)))
+    assert abs(LA.LinAlg_VectorNorm2(v) - np.linalg.norm(xv)) <= 1e-13 * np.linalg.norm(xv)
+
+
+def test_complex_adds_skip_zero_parts():
+    A = LA.LinAlg_CreateMatrix(None, 4)
+    LA.LinAlg_AddComplexInMatrix(2.0, 0.0, A, 0, 0, 1, 1)
+    LA.LinAlg_AddComplexInMatrix(0.0, 3.0, A, 2, 0, 3, 1)
+    LA.LinAlg_AddComplexInMatrix(1.0, 1.0, A, 2, 2, 3, 3)
+    LA.LinAlg_AddComplexInMatrix(1.0, 1.0, A, 0, 2, 1, 3)
+    ip, ix, dv = A.csr()
+    dense = np.zeros((4, 4))
+    for i in range(4):
+        for k in range(ip[i], ip[i + 1]):
+            dense[i, ix[k]] = dv[k]
+    # (0,0),(1,1) real 2; rows 2/3 to cols 0/1 imaginary only
+    assert dense[0, 0] == 2 and dense[1, 1] == 2 and dense[0, 1] == 0
+    assert dense[2, 1] == -3 and dense[3, 0] == 3
+    assert ip[-1] == 2 + 2 + 4 + 4
