@@ -218,6 +218,23 @@ int gb300_event_elapsed(gb300_ctx *ctx, int slot0, int slot1, float *ms);
    vectors) over `reps` launches timed with CUDA events after a warm-up. */
 int gb300_bench_spmv(gb300_matrix *A, int precision, int reps, double *ms);
 
+/* ---- residual without device allocation ------------------------------ */
+/* No counterpart in the reference: an entry point for callers that cannot
+   allocate GPU memory once they are running (an application that reserves
+   all device memory at start-up, or a latency-bound loop in which
+   cudaMalloc's implicit synchronisation is not acceptable).  Computes
+   r = b - A x (device vectors, r distinct from x and b) and *norm =
+   ||r||_2 in FP64 with scratch in a fixed device array: A must already be
+   assembled and have at most 33,554,432 rows (GB300_ERR_CAPACITY
+   otherwise).  The array (128 KiB) is held on every GPU that loads the
+   library until the process exits.  The first call on a device looks up
+   the array's address; make it before any stream capture.  All calls share
+   the array, so calls that overlap on the GPU race and must be serialized
+   by the caller. */
+int gb300_residual_noalloc(gb300_matrix *A, const gb300_vector *x,
+                           const gb300_vector *b, gb300_vector *r,
+                           double *norm);
+
 /* ---- solve ------------------------------------------------------------ */
 /* LinAlg_Solve -> solve_matrix (Sparskit.cpp:108-634) on the GPU.  A and b
    are not modified (Sparskit scales them in place; here scaling acts on
