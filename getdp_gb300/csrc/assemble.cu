@@ -494,7 +494,11 @@ int generate_pattern(gb300_matrix *A, const gb300_term_batch *t)
   A->hr.clear();
   A->hc.clear();
   A->hv.clear();
-  return build_pattern_from_elements(A, t->n_elems, nloc, B.p_edofs, flag, cplx);
+  GB_TRY(build_pattern_from_elements(A, t->n_elems, nloc, B.p_edofs, flag, cplx));
+  // the elasticity tables number unknowns component by component; the
+  // solver checks the block structure itself before relying on it
+  A->block3 = (t->kind == GB300_TERM_TET10_ELASTICITY);
+  return GB300_OK;
 }
 
 int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t)

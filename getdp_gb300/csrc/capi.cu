@@ -606,6 +606,8 @@ int gb300_matrix_set_csr(gb300_matrix *A, long long nnz, const int *rowptr,
   A->nnz = nnz;
   A->csr_valid = true;
   A->val32_valid = false;
+  A->block3 = false;
+  A->bsr_var32 = A->bsr_var64 = -1;
   A->hr.clear();
   A->hc.clear();
   A->hv.clear();

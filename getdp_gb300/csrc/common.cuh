@@ -101,6 +101,36 @@ template <typename T> __device__ __forceinline__ T ld_stream(const T *p)
   return __ldcs(p);
 }
 
+// Partial dot product of one CSR row with x for the TPR lanes that share
+// the row: each lane first issues U independent (column, value) loads, then
+// the U gathers of x through the read-only path, then the multiply-adds, so
+// a warp keeps U memory requests in flight instead of one dependent chain.
+template <int TPR, int U, typename ACC, typename V, typename XT>
+__device__ __forceinline__ ACC csr_row_dot(int s, int e, int lane,
+                                           const int *__restrict__ col,
+                                           const V *__restrict__ val,
+                                           const XT *__restrict__ x)
+{
+  ACC sum = 0;
+  for(int k0 = s + lane; k0 < e; k0 += TPR * U) {
+    int c[U];
+    V v[U];
+#pragma unroll
+    for(int u = 0; u < U; u++) {
+      int k = k0 + u * TPR;
+      bool in = k < e;
+      c[u] = in ? __ldcs(col + k) : 0;
+      v[u] = in ? __ldcs(val + k) : (V)0;
+    }
+    XT xv[U];
+#pragma unroll
+    for(int u = 0; u < U; u++) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+    for(int u = 0; u < U; u++) sum += (ACC)v[u] * (ACC)xv[u];
+  }
+  return sum;
+}
+
 // position of column c in the sorted row [lo, hi) of col[], or -1
 __device__ __forceinline__ int find_col(const int *__restrict__ col, int lo,
                                         int hi, int c)
@@ -154,6 +184,10 @@ struct gb300_matrix {
   bool csr_valid = false;
   bool val32_valid = false;
   int tpr = 32;  // threads per row for the CSR kernels
+  // three-component system in GetDP's component-major numbering (set by the
+  // elasticity Generate hook): the CG may iterate on a 3x3-blocked copy
+  bool block3 = false;
+  int bsr_var32 = -1, bsr_var64 = -1;  // tuned SpMV launch shapes (-1: not yet)
   // ILU(0) state, created on demand by the solver
   gb::ilu_data *ilu = nullptr;
 };

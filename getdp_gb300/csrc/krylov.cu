@@ -226,8 +226,7 @@ k_cg_spmv(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
     XT sum = 0;
     if(row < n) {
       int s = rowptr[row], e = rowptr[row + 1];
-      for(int k = s + lane; k < e; k += TPR)
-        sum += (XT)ld_stream(val + k) * p[ld_stream(col + k)];
+      sum = csr_row_dot<TPR, (TPR >= 16 ? 4 : 2), XT>(s, e, lane, col, val, p);
     }
 #pragma unroll
     for(int o = TPR / 2; o > 0; o >>= 1)
@@ -254,15 +253,14 @@ static void cg_spmv(const gb300_matrix *A, const V *val, const XT *p, XT *q,
   }
 }
 
-// Runs CG on (A with values `val`) y = rhs, starting from y = 0, to
-// ||r|| <= rtol ||rhs||.  T is the vector type (double, or float with
-// float values).  Returns the final state in *hs.
-template <typename V, typename T>
-static int cg_run(const gb300_matrix *A, const V *val, const T *rhs, T *y,
-                  double rtol, int maxit, CgState *hs, Work &W)
+// Runs CG on the operator applied by spmv_dot(p, q, part, S, stream)
+// (q = A p with the partials of <p, q>), y = rhs from y = 0, to
+// ||r|| <= rtol ||rhs||.  T is the vector type, n the vector length.
+// Returns the final state in *hs.
+template <typename T, typename SPMV>
+static int cg_core(cudaStream_t st, int n, SPMV spmv_dot, const T *rhs, T *y,
+                   double rtol, int maxit, CgState *hs, Work &W)
 {
-  cudaStream_t st = A->ctx->stream;
-  int n = A->n;
   T *r = (T *)W.vec(0, n * sizeof(T));
   T *p = (T *)W.vec(1, n * sizeof(T));
   T *q = (T *)W.vec(2, n * sizeof(T));
@@ -288,7 +286,7 @@ static int cg_run(const gb300_matrix *A, const V *val, const T *rhs, T *y,
   cudaGraphExec_t exec;
   GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   for(int it = 0; it < batch; it++) {
-    cg_spmv<V, T>(A, val, p, q, part, S, st);
+    spmv_dot(p, q, part, S, st);
     k_cg_alpha<<<1, 256, 0, st>>>(S, part);
     k_cg_update<T><<<kReduceBlocks, 256, 0, st>>>(n, S, y, r, p, q, part);
     k_cg_check<<<1, 256, 0, st>>>(S, part);
@@ -330,7 +328,34 @@ int bench_spmv(gb300_matrix *A, int precision, int reps, double *ms)
   GB_CUDA(cudaEventCreate(&e0));
   GB_CUDA(cudaEventCreate(&e1));
   float t = 0.f;
-  if(precision == 0) {
+  Bsr3 B;
+  if(A->block3 &&
+     bsr_build(A, A->val.p, precision == 0, precision != 0, B) == GB300_OK &&
+     bsr_tune(A, B, st) == GB300_OK) {
+    // the kernel the CG runs on a 3-component system: 3x3 blocks
+    int n4 = 4 * B.nn;
+    if(precision == 0) {
+      double *p = (double *)W.vec(0, sizeof(double) * n4);
+      double *q = (double *)W.vec(1, sizeof(double) * n4);
+      if(!p || !q) return GB300_ERR_CUDA;
+      k_copy<double><<<grid_for(n4, 256), 256, 0, st>>>(n4, B.val64.p, p);
+      for(int i = 0; i < 3; i++) bsr_spmv_dot64(B, p, q, part, &S->active, st);
+      GB_CUDA(cudaEventRecord(e0, st));
+      for(int i = 0; i < reps; i++) bsr_spmv_dot64(B, p, q, part, &S->active, st);
+      GB_CUDA(cudaEventRecord(e1, st));
+    }
+    else {
+      float *p = (float *)W.vec(0, sizeof(float) * n4);
+      float *q = (float *)W.vec(1, sizeof(float) * n4);
+      if(!p || !q) return GB300_ERR_CUDA;
+      k_copy<float><<<grid_for(n4, 256), 256, 0, st>>>(n4, B.val32.p, p);
+      for(int i = 0; i < 3; i++) bsr_spmv_dot32(B, p, q, part, &S->active, st);
+      GB_CUDA(cudaEventRecord(e0, st));
+      for(int i = 0; i < reps; i++) bsr_spmv_dot32(B, p, q, part, &S->active, st);
+      GB_CUDA(cudaEventRecord(e1, st));
+    }
+  }
+  else if(precision == 0) {
     double *p = (double *)W.vec(0, sizeof(double) * n);
     double *q = (double *)W.vec(1, sizeof(double) * n);
     if(!p || !q) return GB300_ERR_CUDA;
@@ -474,14 +499,13 @@ __global__ void k_fold_all(int n, double *__restrict__ x, const float *__restric
   if(i < n) x[i] += (double)x32[i];
 }
 
-static int cg_mixed(const gb300_matrix *A, const double *val, const double *rhs,
-                    double *x, double rtol, int maxit, CgState *hs, Work &W)
+// spmv32(p, q, part, S, st): FP32 q = A p with partial <p, q>;
+// res64(x, b, r, part, flag, st): FP64 r = b - A x with partial ||r||^2
+template <typename SPMV32, typename RES64>
+static int cg_mixed_core(cudaStream_t st, int n, SPMV32 spmv32, RES64 res64,
+                         const double *rhs, double *x, double rtol, int maxit,
+                         CgState *hs, Work &W)
 {
-  cudaStream_t st = A->ctx->stream;
-  int n = A->n;
-  DevBuf<float> v32;
-  GB_TRY(v32.alloc(A->nnz > 0 ? A->nnz : 1));
-  k_convert<float, double><<<grid_for(A->nnz, 256), 256, 0, st>>>(A->nnz, val, v32.p);
   float *r32 = (float *)W.vec(0, n * sizeof(float));
   float *p32 = (float *)W.vec(1, n * sizeof(float));
   float *q32 = (float *)W.vec(2, n * sizeof(float));
@@ -505,14 +529,16 @@ static int cg_mixed(const gb300_matrix *A, const double *val, const double *rhs,
   cudaGraphExec_t exec;
   GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   for(int it = 0; it < batch; it++) {
-    cg_spmv<float, float>(A, v32.p, p32, q32, part, S, st);
+    spmv32(p32, q32, part, S, st);
     k_cg_alpha<<<1, 256, 0, st>>>(S, part);
     k_cg_update<float><<<kReduceBlocks, 256, 0, st>>>(n, S, x32, r32, p32, q32, part);
     k_rcg_check<<<1, 256, 0, st>>>(S, part);
-    k_rcg_fold<<<gs, 256, 0, st>>>(n, S, x, x32);
-    residual64_guarded(A, val, x, rhs, r64, part, &S->update, st);
+    // the reliable-update branch: kernels return at once unless S->update
+    // (about one step in 300), so they get the small fixed grid
+    k_rcg_fold<<<kReduceBlocks, 256, 0, st>>>(n, S, x, x32);
+    res64(x, rhs, r64, part, &S->update, st);
     k_rcg_after<<<1, 256, 0, st>>>(S, part);
-    k_rcg_convert<<<gs, 256, 0, st>>>(n, S, r64, r32);
+    k_rcg_convert<<<kReduceBlocks, 256, 0, st>>>(n, S, r64, r32);
     k_cg_p<float><<<gs, 256, 0, st>>>(n, S, p32, r32);
   }
   GB_CUDA(cudaStreamEndCapture(st, &graph));
@@ -677,23 +703,71 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
   if(p->algorithm == 1 && p->preconditioner != 6) {
     // CG; Preconditioner 0 and 8 (DIAGONAL stores alu = 1: the identity,
     // Sparskit.cpp:338-354) both leave the operator unchanged
-    if(p->precision == 0) {
-      CgState hs;
-      GB_TRY(cg_run<double, double>(A, val, rhs, x, p->stopping_test,
-                                    p->nb_iter_max, &hs, W));
-      info->status = hs.status;
-      info->iterations = hs.its;
-      info->residual_estimate = hs.res;
+    bool mixed = (p->precision != 0);
+    CgState hs;
+    Bsr3 B;
+    bool blocked = A->block3 &&
+                   bsr_build(A, val, true, mixed, B) == GB300_OK &&
+                   bsr_tune(A, B, st) == GB300_OK;
+    if(blocked) {
+      // node-major 3x3 blocks: vectors of 4 entries per node
+      int nn = B.nn, n4 = 4 * nn;
+      double *rhs4 = (double *)W.vec(20, sizeof(double) * n4);
+      double *x4 = (double *)W.vec(21, sizeof(double) * n4);
+      if(!rhs4 || !x4) return GB300_ERR_CUDA;
+      to_nodes64(nn, rhs, rhs4, st);
+      if(!mixed) {
+        auto spmv = [&](const double *pp, double *qq, double *part,
+                        const CgState *S, cudaStream_t s) {
+          bsr_spmv_dot64(B, pp, qq, part, &S->active, s);
+        };
+        GB_TRY(cg_core<double>(st, n4, spmv, rhs4, x4, p->stopping_test,
+                               p->nb_iter_max, &hs, W));
+      }
+      else {
+        auto spmv = [&](const float *pp, float *qq, double *part,
+                        const CgState *S, cudaStream_t s) {
+          bsr_spmv_dot32(B, pp, qq, part, &S->active, s);
+        };
+        auto res = [&](const double *xx, const double *bb, double *rr,
+                       double *part, const int *flag, cudaStream_t s) {
+          bsr_residual64(B, xx, bb, rr, part, flag, s);
+        };
+        GB_TRY(cg_mixed_core(st, n4, spmv, res, rhs4, x4, p->stopping_test,
+                             p->nb_iter_max, &hs, W));
+      }
+      from_nodes64(nn, x4, x, st);
+    }
+    else if(!mixed) {
+      auto spmv = [&](const double *pp, double *qq, double *part,
+                      const CgState *S, cudaStream_t s) {
+        cg_spmv<double, double>(A, val, pp, qq, part, S, s);
+      };
+      GB_TRY(cg_core<double>(st, n, spmv, rhs, x, p->stopping_test,
+                             p->nb_iter_max, &hs, W));
     }
     else {
-      // FP32 CG with FP64 reliable updates (residual replacement)
-      CgState hs;
-      GB_TRY(cg_mixed(A, val, rhs, x, p->stopping_test, p->nb_iter_max, &hs, W));
-      info->status = hs.status;
-      info->iterations = hs.its;
+      DevBuf<float> v32;
+      GB_TRY(v32.alloc(A->nnz > 0 ? A->nnz : 1));
+      k_convert<float, double><<<grid_for(A->nnz, 256), 256, 0, st>>>(A->nnz, val, v32.p);
+      const float *v32p = v32.p;
+      auto spmv = [&](const float *pp, float *qq, double *part,
+                      const CgState *S, cudaStream_t s) {
+        cg_spmv<float, float>(A, v32p, pp, qq, part, S, s);
+      };
+      auto res = [&](const double *xx, const double *bb, double *rr,
+                     double *part, const int *flag, cudaStream_t s) {
+        residual64_guarded(A, val, xx, bb, rr, part, flag, s);
+      };
+      GB_TRY(cg_mixed_core(st, n, spmv, res, rhs, x, p->stopping_test,
+                           p->nb_iter_max, &hs, W));
+    }
+    info->status = hs.status;
+    info->iterations = hs.its;
+    info->residual_estimate = hs.res;
+    if(mixed) {
       info->inner_iterations = hs.its - 1;
       info->refinement_steps = hs.updates;
-      info->residual_estimate = hs.res;
     }
   }
   else if(p->algorithm == 8 || p->algorithm == 9 ||

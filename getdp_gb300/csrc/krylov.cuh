@@ -28,6 +28,28 @@ int norm2_dev(int n, const double *v, double *out, Work &W, cudaStream_t st);
 
 int bench_spmv(gb300_matrix *A, int precision, int reps, double *ms);
 
+// node-blocked 3 x 3 copy of a three-component system (bsr.cu)
+struct Bsr3 {
+  int nn = 0;          // block rows (nodes)
+  long long nblk = 0;  // blocks
+  DevBuf<int> ptr, col;
+  DevBuf<double> val64;  // 9 planes of nblk values
+  DevBuf<float> val32;
+  int var32 = 0, var64 = 0;  // SpMV launch shapes chosen by bsr_tune
+};
+int bsr_build(const gb300_matrix *A, const double *val, bool want64,
+              bool want32, Bsr3 &B);
+// pick the fastest SpMV launch shape for this matrix (cached in A)
+int bsr_tune(gb300_matrix *A, Bsr3 &B, cudaStream_t st);
+void to_nodes64(int nn, const double *in, double *out, cudaStream_t st);
+void from_nodes64(int nn, const double *in, double *out, cudaStream_t st);
+void bsr_spmv_dot32(const Bsr3 &B, const float *p, float *q, double *part,
+                    const int *flag, cudaStream_t st);
+void bsr_spmv_dot64(const Bsr3 &B, const double *p, double *q, double *part,
+                    const int *flag, cudaStream_t st);
+void bsr_residual64(const Bsr3 &B, const double *x, const double *b, double *r,
+                    double *part, const int *flag, cudaStream_t st);
+
 int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
                 double *x, const gb300_solver_params *p, gb300_solve_info *info,
                 Work &W);

@@ -287,6 +287,8 @@ int build_pattern_from_elements(gb300_matrix *A, int ne, int nloc,
   A->nnz = nnz;
   A->csr_valid = true;
   A->val32_valid = false;
+  A->block3 = false;
+  A->bsr_var32 = A->bsr_var64 = -1;
   choose_tpr(A);
   GB_CUDA(cudaStreamSynchronize(st));
   return GB300_OK;
@@ -442,6 +444,8 @@ int build_csr_from_coo(gb300_matrix *A, long long m, const int *d_r,
   A->nnz = nnz;
   A->csr_valid = true;
   A->val32_valid = false;
+  A->block3 = false;
+  A->bsr_var32 = A->bsr_var64 = -1;
   choose_tpr(A);
   return GB300_OK;
 }
@@ -477,8 +481,7 @@ k_spmv(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
     ACC sum = 0;
     if(row < n) {
       int s = rowptr[row], e = rowptr[row + 1];
-      for(int k = s + lane; k < e; k += TPR)
-        sum += (ACC)ld_stream(val + k) * x[ld_stream(col + k)];
+      sum = csr_row_dot<TPR, (TPR >= 16 ? 4 : 2), ACC>(s, e, lane, col, val, x);
     }
 #pragma unroll
     for(int o = TPR / 2; o > 0; o >>= 1)
