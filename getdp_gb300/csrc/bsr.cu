@@ -85,17 +85,22 @@ int bsr_build(const gb300_matrix *A, const double *val, bool want64,
   long long nblk = nnz_c0 / 3;
   B.nn = nn;
   B.nblk = nblk;
+  // plane stride: a multiple of 4 entries plus slack, so that every bulk
+  // copy of a 4-aligned block range starts and ends on 16 bytes
+  B.pstride = ((nblk + 3) & ~3LL) + 4;
   GB_TRY(B.ptr.alloc(nn + 1));
-  GB_TRY(B.col.alloc(nblk > 0 ? nblk : 1));
-  if(want64) GB_TRY(B.val64.alloc(9 * (nblk > 0 ? nblk : 1)));
-  if(want32) GB_TRY(B.val32.alloc(9 * (nblk > 0 ? nblk : 1)));
+  GB_TRY(B.col.alloc(B.pstride));
+  if(want64) GB_TRY(B.val64.alloc(9 * B.pstride));
+  if(want32) GB_TRY(B.val32.alloc(9 * B.pstride));
+  GB_TRY(B.err.alloc(1));
+  GB_CUDA(cudaMemsetAsync(B.err.p, 0, sizeof(int), st));
   DevBuf<int> bad;
   GB_TRY(bad.alloc(1));
   GB_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
   k_bsr_ptr<<<grid_for(nn + 1, 256), 256, 0, st>>>(nn, A->rowptr.p, B.ptr.p);
   k_bsr_build<<<grid_for(nn, 8), 256, 0, st>>>(nn, A->rowptr.p, A->col.p, val,
                                                 B.col.p, want64 ? B.val64.p : nullptr,
-                                                want32 ? B.val32.p : nullptr, nblk,
+                                                want32 ? B.val32.p : nullptr, B.pstride,
                                                 bad.p);
   GB_CUDA(cudaGetLastError());
   int hb = 0;
@@ -235,10 +240,245 @@ k_bsr_spmv(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
   }
 }
 
+// ---------------------------------------------------------------------------
+// TMA-staged variant: each CTA walks tiles of kTileRows block rows; one
+// elected thread copies a tile's nine value planes and column indices from
+// HBM to shared memory with cp.async.bulk (completion counted on an
+// mbarrier), two tiles in flight; all threads compute from shared memory,
+// so only the x gathers (L2-resident vectors) still wait on memory.
+// Bulk copies need 16-byte aligned addresses and sizes: tile ranges are
+// widened to multiples of four blocks (planes are padded accordingly).
+// Every wait is bounded; on time-out the CTA records an error, waits
+// (bounded) for its own copies and returns.
+// ---------------------------------------------------------------------------
+constexpr int kTileRows = 16;
+constexpr int kTileCap = 1024;  // blocks per tile (+4 alignment slack)
+constexpr int kTmaThreads = 256;
+constexpr long long kWaitLimit = 1LL << 26;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p)
+{
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, int count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar,
+                                               unsigned bytes)
+{
+  asm volatile(
+    "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+    "r"(bytes)
+    : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
+                                         unsigned bytes, unsigned long long *bar)
+{
+  asm volatile(
+    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+    "[%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+    "l"(src), "r"(bytes), "r"(smem_addr(bar))
+    : "memory");
+}
+
+// true when the phase with the given parity has completed
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar,
+                                              unsigned parity)
+{
+  unsigned ok;
+  asm volatile(
+    "{\n .reg .pred p;\n"
+    " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+    " selp.u32 %0, 1, 0, p;\n}"
+    : "=r"(ok)
+    : "r"(smem_addr(bar)), "r"(parity)
+    : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar,
+                                                  unsigned parity)
+{
+  for(long long i = 0; i < kWaitLimit; i++)
+    if(mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+template <typename T> struct TmaTile {
+  T val[9][kTileCap + 4];
+  int col[kTileCap + 4];
+};
+
+template <int MODE, typename T, int LPR>
+__global__ void __launch_bounds__(kTmaThreads)
+k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
+               const T *__restrict__ val, long long pstride,
+               const T *__restrict__ p, const T *__restrict__ bvec,
+               T *__restrict__ y, double *__restrict__ part, const int *flag,
+               int *__restrict__ err)
+{
+  if(flag && !*flag) return;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  TmaTile<T> *stage = (TmaTile<T> *)smem_raw;
+  __shared__ __align__(8) unsigned long long bar[2];
+  __shared__ int tile_k0[2], tile_n[2];  // aligned first block, blocks copied
+  const int ntiles = (nn + kTileRows - 1) / kTileRows;
+  const int tid = threadIdx.x;
+
+  if(tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  // thread 0 issues the copies of tile t into stage s (or marks it direct)
+  auto issue = [&](int t, int s) {
+    int r0 = t * kTileRows;
+    int r1 = min(r0 + kTileRows, nn);
+    int k0 = ptr[r0], k1 = ptr[r1];
+    int k0a = k0 & ~3, k1a = (k1 + 3) & ~3;
+    int nb = k1a - k0a;
+    tile_k0[s] = k0a;
+    if(nb > kTileCap + 4 || nb <= 0) {
+      tile_n[s] = -1;  // too long for the stage: read this tile directly
+      return;
+    }
+    tile_n[s] = nb;
+    unsigned bytes = (unsigned)(9 * nb * sizeof(T) + nb * sizeof(int));
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&bar[s], bytes);
+    for(int c = 0; c < 9; c++)
+      bulk_g2s(stage[s].val[c], val + c * pstride + k0a, nb * sizeof(T), &bar[s]);
+    bulk_g2s(stage[s].col, col + k0a, nb * sizeof(int), &bar[s]);
+  };
+
+  int t0 = blockIdx.x;
+  if(tid == 0) {
+    if(t0 < ntiles) issue(t0, 0);
+    if(t0 + gridDim.x < ntiles) issue(t0 + gridDim.x, 1);
+  }
+  __syncthreads();
+
+  const int lane = tid % LPR, sub = tid / LPR;
+  const int rows_per_pass = kTmaThreads / LPR;
+  double red = 0.;
+  unsigned phase[2] = {0u, 0u};
+  int i = 0;
+  bool failed = false;
+  for(int t = t0; t < ntiles; t += gridDim.x, i++) {
+    int s = i & 1;
+    bool direct = tile_n[s] < 0;
+    if(!direct) {
+      bool ok = mbar_wait_bounded(&bar[s], phase[s]);
+      if(__syncthreads_or(!ok)) {
+        failed = true;
+        break;
+      }
+      phase[s] ^= 1u;
+    }
+    int k0a = tile_k0[s];
+    const T *sv = stage[s].val[0];
+    int r0 = t * kTileRows, r1 = min(r0 + kTileRows, nn);
+    for(int a = r0 + sub; a - sub < r1; a += rows_per_pass) {
+      T y0 = 0, y1 = 0, y2 = 0;
+      if(a < r1) {
+        int s0 = ptr[a], e0 = ptr[a + 1];
+        for(int k = s0 + lane; k < e0; k += LPR) {
+          int b;
+          T v[9];
+          if(!direct) {
+            int kk = k - k0a;
+            b = stage[s].col[kk];
+#pragma unroll
+            for(int c = 0; c < 9; c++) v[c] = sv[c * (kTileCap + 4) + kk];
+          }
+          else {
+            b = __ldg(col + k);
+#pragma unroll
+            for(int c = 0; c < 9; c++) v[c] = __ldg(val + c * pstride + k);
+          }
+          auto xb = Vec4<T>::load(p + 4 * (size_t)b);
+          y0 += v[0] * xb.x + v[1] * xb.y + v[2] * xb.z;
+          y1 += v[3] * xb.x + v[4] * xb.y + v[5] * xb.z;
+          y2 += v[6] * xb.x + v[7] * xb.y + v[8] * xb.z;
+        }
+      }
+#pragma unroll
+      for(int o = LPR / 2; o > 0; o >>= 1) {
+        y0 += __shfl_down_sync(0xffffffffu, y0, o, LPR);
+        y1 += __shfl_down_sync(0xffffffffu, y1, o, LPR);
+        y2 += __shfl_down_sync(0xffffffffu, y2, o, LPR);
+      }
+      if(lane == 0 && a < r1) {
+        size_t o = 4 * (size_t)a;
+        if(MODE == 1) {
+          T q0 = bvec[o] - y0, q1 = bvec[o + 1] - y1, q2 = bvec[o + 2] - y2;
+          y[o] = q0;
+          y[o + 1] = q1;
+          y[o + 2] = q2;
+          y[o + 3] = 0;
+          red += (double)q0 * q0 + (double)q1 * q1 + (double)q2 * q2;
+        }
+        else {
+          y[o] = y0;
+          y[o + 1] = y1;
+          y[o + 2] = y2;
+          y[o + 3] = 0;
+          if(MODE == 2)
+            red += (double)p[o] * y0 + (double)p[o + 1] * y1 + (double)p[o + 2] * y2;
+        }
+      }
+    }
+    __syncthreads();  // every thread is done with stage s
+    if(tid == 0 && t + 2 * (int)gridDim.x < ntiles) issue(t + 2 * gridDim.x, s);
+    __syncthreads();
+  }
+  if(failed) {
+    // record, then let the copies still in flight land before leaving
+    if(tid == 0) {
+      atomicExch(err, 1);
+      for(int s = 0; s < 2; s++)
+        if(tile_n[s] > 0) mbar_wait_bounded(&bar[s], phase[s]);
+    }
+    __syncthreads();
+    return;
+  }
+  if(MODE != 0) {
+    double s = block_sum<double, kTmaThreads>(red);
+    if(tid == 0) part[blockIdx.x] = s;
+    // the consumers sum a fixed number of partials
+    if(blockIdx.x == 0)
+      for(int b = gridDim.x + tid; b < kReduceBlocks; b += blockDim.x) part[b] = 0.;
+  }
+}
+
 // launch shapes the tuner chooses from, as (lanes per block row, blocks in
 // flight per lane, streaming loads): 0 (8,2,cs) 1 (8,2,ldg) 2 (16,2,cs)
-// 3 (16,2,ldg) 4 (8,4,ldg) 5 (32,2,ldg)
-constexpr int kBsrVariants = 6;
+// 3 (16,2,ldg) 4 (8,4,ldg) 5 (32,2,ldg); 6 and 7: the TMA-staged kernel
+// with 16 and 8 lanes per block row
+constexpr int kBsrVariants = 8;
+
+template <int MODE, typename T, int LPR>
+static void launch_tma(const Bsr3 &B, const T *val, const T *p, const T *b,
+                       T *y, double *part, const int *flag, cudaStream_t st)
+{
+  size_t smem = 2 * sizeof(TmaTile<T>);
+  static bool configured = false;  // per instantiation
+  if(!configured) {
+    cudaFuncSetAttribute(k_bsr_spmv_tma<MODE, T, LPR>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = true;
+  }
+  int per_sm = sizeof(T) == 4 ? 2 : 1;
+  k_bsr_spmv_tma<MODE, T, LPR><<<152 * per_sm, kTmaThreads, smem, st>>>(
+    B.nn, B.ptr.p, B.col.p, val, B.pstride, p, b, y, part, flag, B.err.p);
+}
 
 template <int MODE, typename T>
 static void launch_bsr(int variant, const Bsr3 &B, const T *val, const T *p,
@@ -247,8 +487,10 @@ static void launch_bsr(int variant, const Bsr3 &B, const T *val, const T *p,
 {
 #define GB_BSR(L, U, C)                                                       \
   k_bsr_spmv<MODE, T, L, U, C><<<kReduceBlocks, 256, 0, st>>>(               \
-    B.nn, B.ptr.p, B.col.p, val, B.nblk, p, b, y, part, flag)
+    B.nn, B.ptr.p, B.col.p, val, B.pstride, p, b, y, part, flag)
   switch(variant) {
+  case 6: launch_tma<MODE, T, 16>(B, val, p, b, y, part, flag, st); break;
+  case 7: launch_tma<MODE, T, 8>(B, val, p, b, y, part, flag, st); break;
   case 1: GB_BSR(8, 2, 0); break;
   case 2: GB_BSR(16, 2, 1); break;
   case 3: GB_BSR(16, 2, 0); break;
@@ -275,27 +517,88 @@ void bsr_residual64(const Bsr3 &B, const double *x, const double *b, double *r,
   launch_bsr<1, double>(B.var64, B, B.val64.p, x, b, r, part, flag, st);
 }
 
+template <typename T>
+__global__ void k_tune_fill(size_t n4, T *a, T *b)
+{
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= n4) return;
+  bool pad = (i & 3) == 3;
+  a[i] = pad ? (T)0 : (T)(1.0 + 0.125 * (double)(i % 7));
+  b[i] = pad ? (T)0 : (T)(0.5 - 0.0625 * (double)(i % 5));
+}
+
+// flags a result that differs from the reference beyond tol * max|ref|
+template <typename T>
+__global__ void k_tune_check(size_t n4, const T *q, const T *ref, double scale,
+                             double tol, int *bad)
+{
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= n4) return;
+  double d = fabs((double)q[i] - (double)ref[i]);
+  if(!(d <= tol * scale)) atomicExch(bad, 1);
+}
+
+template <typename T>
+__global__ void k_absmax(size_t n4, const T *q, unsigned long long *out)
+{
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= n4) return;
+  double v = fabs((double)q[i]);
+  atomicMax(out, (unsigned long long)__double_as_longlong(v));
+}
+
 // Times every launch shape on this matrix (alternating between two input
-// vectors, as in a CG where p changes every step) and keeps the fastest.
+// vectors, as in a CG where p changes every step) and keeps the fastest of
+// those whose result matches the plain kernel's (a variant that disagrees,
+// or whose staged copies time out, is never chosen).
 template <typename T>
 static int tune_one(Bsr3 &B, const T *val, int *out, cudaStream_t st)
 {
   size_t n4 = 4 * (size_t)B.nn;
-  DevBuf<T> pa, pb, q;
+  DevBuf<T> pa, pb, q, qref;
   DevBuf<double> part;
+  DevBuf<int> bad;
+  DevBuf<unsigned long long> amax;
   GB_TRY(pa.alloc(n4));
   GB_TRY(pb.alloc(n4));
   GB_TRY(q.alloc(n4));
+  GB_TRY(qref.alloc(n4));
   GB_TRY(part.alloc(kReduceBlocks));
-  GB_CUDA(cudaMemsetAsync(pa.p, 0, n4 * sizeof(T), st));
-  GB_CUDA(cudaMemsetAsync(pb.p, 0, n4 * sizeof(T), st));
+  GB_TRY(bad.alloc(1));
+  GB_TRY(amax.alloc(1));
+  k_tune_fill<T><<<grid_for((long long)n4, 256), 256, 0, st>>>(n4, pa.p, pb.p);
+  // the reference: the plain (non-staged) kernel, variant 1
+  launch_bsr<2, T>(1, B, val, pa.p, nullptr, qref.p, part.p, nullptr, st);
+  GB_CUDA(cudaMemsetAsync(amax.p, 0, sizeof(unsigned long long), st));
+  k_absmax<T><<<grid_for((long long)n4, 256), 256, 0, st>>>(n4, qref.p, amax.p);
+  unsigned long long hmax = 0;
+  GB_CUDA(cudaMemcpyAsync(&hmax, amax.p, sizeof(hmax), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  double scale;
+  memcpy(&scale, &hmax, sizeof(scale));
+  double tol = sizeof(T) == 4 ? 1e-4 : 1e-12;
   cudaEvent_t e0, e1;
   GB_CUDA(cudaEventCreate(&e0));
   GB_CUDA(cudaEventCreate(&e1));
   float best = 1e30f;
-  int bestv = 0;
+  int bestv = 1;
   for(int v = 0; v < kBsrVariants; v++) {
+    GB_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
+    GB_CUDA(cudaMemsetAsync(B.err.p, 0, sizeof(int), st));
     launch_bsr<2, T>(v, B, val, pa.p, nullptr, q.p, part.p, nullptr, st);
+    k_tune_check<T><<<grid_for((long long)n4, 256), 256, 0, st>>>(n4, q.p, qref.p,
+                                                                 scale, tol, bad.p);
+    int hb = 0, he = 0;
+    GB_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemcpyAsync(&he, B.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    GB_CUDA(cudaGetLastError());
+    if(hb || he) {
+      if(getenv("GB300_TUNE_VERBOSE"))
+        fprintf(stderr, "bsr spmv variant %d rejected (%s)\n", v,
+                hb ? "result differs" : "staged copy timed out");
+      continue;
+    }
     GB_CUDA(cudaEventRecord(e0, st));
     for(int r = 0; r < 6; r++)
       launch_bsr<2, T>(v, B, val, (r & 1) ? pb.p : pa.p, nullptr, q.p, part.p,

@@ -32,10 +32,12 @@ int bench_spmv(gb300_matrix *A, int precision, int reps, double *ms);
 struct Bsr3 {
   int nn = 0;          // block rows (nodes)
   long long nblk = 0;  // blocks
+  long long pstride = 0;  // stride between value planes (padded)
   DevBuf<int> ptr, col;
   DevBuf<double> val64;  // 9 planes of nblk values
   DevBuf<float> val32;
   int var32 = 0, var64 = 0;  // SpMV launch shapes chosen by bsr_tune
+  DevBuf<int> err;           // set by a staged SpMV whose copies timed out
 };
 int bsr_build(const gb300_matrix *A, const double *val, bool want64,
               bool want32, Bsr3 &B);
