@@ -41,7 +41,7 @@ UNIT = "s"
 # system, as counted by the GPU FP64 CG, which runs the same iteration (its
 # counts equal the oracle's on every golden case).  Used by the reference
 # arm to extrapolate its per-iteration time to the full solve.
-FP64_CG_ITERATIONS = {48: None}
+FP64_CG_ITERATIONS = {48: 2902}
 
 
 def parse():
@@ -54,9 +54,12 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 comparison solve (profiling runs)")
-    ap.add_argument("--profile", choices=["spmv32", "spmv64", "generate"],
+    ap.add_argument("--profile", choices=["spmv32", "spmv64", "generate", "step"],
                     help="minimal run for ncu: one Generate, then 3 warm-up "
-                         "and 3 timed launches of the chosen kernel")
+                         "and 3 timed launches of the chosen kernel; 'step': "
+                         "one warm-up step, then one Generate + mixed solve "
+                         "capped at --profile-iterations CG iterations")
+    ap.add_argument("--profile-iterations", type=int, default=64)
     return ap.parse_args()
 
 
@@ -76,6 +79,15 @@ def profile_run(args):
     if args.profile == "generate":
         G.generate(A, b, terms.batch, pattern=True)
         print(json.dumps({"profile": "generate", "n": args.n, "nnz": A.nnz()}))
+        return
+    if args.profile == "step":
+        x = LA.gVector(dm.n_dof)
+        S = solver_params(True, args.profile_iterations)
+        for _ in range(2):  # the first step also tunes the SpMV
+            G.generate(A, b, terms.batch, pattern=True)
+            info = LA.LinAlg_Solve(A, b, S, x)
+        print(json.dumps({"profile": "step", "n": args.n, "nnz": A.nnz(),
+                          "iterations": info["iterations"]}))
         return
     ms = ctypes.c_double()
     prec = 1 if args.profile == "spmv32" else 0
@@ -392,10 +404,13 @@ def main():
         except Exception:
             traffic = None
     inf = infos[-1]
-    launches_per_it = 9
-    gpu_launches = args.steps * (
-        # generate: pattern (~12 kernels) + values (~3) + solve
-        15 + 12 + inf["iterations"] * launches_per_it)
+    # per step: Generate (pattern ~12 kernels + values) and solve set-up
+    # (~15), then graph replays of 16 CG iterations x 3 kernels (SpMV, step,
+    # direction; a replay ends early at each reliable update) and 5 kernels
+    # per reliable update
+    upd = inf.get("refinement_steps", 0) or 0
+    main_replays = -(-inf["iterations"] // 16) + upd
+    gpu_launches = args.steps * (27 + main_replays * 16 * 3 + upd * 5)
 
     line = {
         "metric": METRIC, "value": per_step, "unit": UNIT, "n_gpus": ws,

@@ -11,6 +11,10 @@
 // reordering of the solver, as Sparskit's RCMK renumbering is; results are
 // permuted back.  The structure is verified while converting; a matrix that
 // does not have it is solved in CSR.
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "krylov.cuh"
 
 namespace gb {
@@ -183,12 +187,16 @@ __device__ __forceinline__ void bsr_block(const int *__restrict__ col,
         mload<CS>(val + 8 * nblk + k) * xb.z;
 }
 
-template <int MODE, typename T, int LPR, int UNR, int CS>
-__global__ void __launch_bounds__(256)
+// MINB: CTAs per SM the register allocation must allow (0 = the compiler's
+// own choice).  The grid is the number of CTAs that are resident at once
+// (resident_grid), so no CTA waits for a second wave.
+template <int MODE, typename T, int LPR, int UNR, int CS, int MINB = 0>
+__global__ void __launch_bounds__(256, MINB)
 k_bsr_spmv(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
            const T *__restrict__ val, long long nblk, const T *__restrict__ p,
            const T *__restrict__ bvec, T *__restrict__ y,
-           double *__restrict__ part, const int *flag)
+           double *__restrict__ part, const int *flag, double *dot_out,
+           unsigned *counter)
 {
   if(flag && !*flag) return;
   const int rows_per_block = 256 / LPR;
@@ -237,7 +245,30 @@ k_bsr_spmv(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
   if(MODE != 0) {
     double s = block_sum<double, 256>(red);
     if(threadIdx.x == 0) part[blockIdx.x] = s;
+    // the consumers sum a fixed number of partials
+    if(blockIdx.x == 0)
+      for(int b = gridDim.x + threadIdx.x; b < kReduceBlocks; b += blockDim.x)
+        part[b] = 0.;
+    // MODE 2 with dot_out: the last block to finish sums <p, y> itself
+    if(MODE == 2 && dot_out && arrive_last(counter)) {
+      double d = sum_partials_l2<256>(part);
+      if(threadIdx.x == 0) *dot_out = d;
+    }
   }
+}
+
+// CTAs of `kernel` that fit on the device at once (at most kReduceBlocks)
+template <typename K>
+static int resident_grid(K kernel, int threads, size_t smem)
+{
+  int dev = 0, sms = 0, per_sm = 0;
+  if(cudaGetDevice(&dev) != cudaSuccess ||
+     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) !=
+       cudaSuccess ||
+     per_sm < 1 || sms < 1)
+    return kReduceBlocks;
+  return per_sm * sms < kReduceBlocks ? per_sm * sms : kReduceBlocks;
 }
 
 // ---------------------------------------------------------------------------
@@ -320,7 +351,7 @@ k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
                const T *__restrict__ val, long long pstride,
                const T *__restrict__ p, const T *__restrict__ bvec,
                T *__restrict__ y, double *__restrict__ part, const int *flag,
-               int *__restrict__ err)
+               int *__restrict__ err, double *dot_out, unsigned *counter)
 {
   if(flag && !*flag) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -447,7 +478,7 @@ k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
         if(tile_n[s] > 0) mbar_wait_bounded(&bar[s], phase[s]);
     }
     __syncthreads();
-    return;
+    red = 0.;  // the result is void (err is set); keep the reduction whole
   }
   if(MODE != 0) {
     double s = block_sum<double, kTmaThreads>(red);
@@ -455,61 +486,85 @@ k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
     // the consumers sum a fixed number of partials
     if(blockIdx.x == 0)
       for(int b = gridDim.x + tid; b < kReduceBlocks; b += blockDim.x) part[b] = 0.;
+    if(MODE == 2 && dot_out && arrive_last(counter)) {
+      double d = sum_partials_l2<kTmaThreads>(part);
+      if(tid == 0) *dot_out = d;
+    }
   }
 }
 
 // launch shapes the tuner chooses from, as (lanes per block row, blocks in
-// flight per lane, streaming loads): 0 (8,2,cs) 1 (8,2,ldg) 2 (16,2,cs)
-// 3 (16,2,ldg) 4 (8,4,ldg) 5 (32,2,ldg); 6 and 7: the TMA-staged kernel
-// with 16 and 8 lanes per block row
-constexpr int kBsrVariants = 8;
+// flight per lane, streaming loads, CTAs per SM the registers must allow):
+// 0 (8,2,cs) 1 (8,2,ldg) 2 (16,2,cs) 3 (16,2,ldg) 4 (8,4,ldg) 5 (32,2,ldg);
+// 6 and 7: the TMA-staged kernel with 16 and 8 lanes per block row;
+// 8 (8,2,ldg,8 CTAs) 9 (8,4,ldg,4 CTAs) 10 (8,2,ldg,4 CTAs)
+constexpr int kBsrVariants = 11;
 
 template <int MODE, typename T, int LPR>
 static void launch_tma(const Bsr3 &B, const T *val, const T *p, const T *b,
-                       T *y, double *part, const int *flag, cudaStream_t st)
+                       T *y, double *part, const int *flag, double *dot_out,
+                       unsigned *counter, cudaStream_t st)
 {
   size_t smem = 2 * sizeof(TmaTile<T>);
-  static bool configured = false;  // per instantiation
-  if(!configured) {
+  static int grid = 0;  // per instantiation
+  if(!grid) {
     cudaFuncSetAttribute(k_bsr_spmv_tma<MODE, T, LPR>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = true;
+    grid = resident_grid(k_bsr_spmv_tma<MODE, T, LPR>, kTmaThreads, smem);
   }
-  int per_sm = sizeof(T) == 4 ? 2 : 1;
-  k_bsr_spmv_tma<MODE, T, LPR><<<152 * per_sm, kTmaThreads, smem, st>>>(
-    B.nn, B.ptr.p, B.col.p, val, B.pstride, p, b, y, part, flag, B.err.p);
+  k_bsr_spmv_tma<MODE, T, LPR><<<grid, kTmaThreads, smem, st>>>(
+    B.nn, B.ptr.p, B.col.p, val, B.pstride, p, b, y, part, flag, B.err.p,
+    dot_out, counter);
+}
+
+template <int MODE, typename T, int L, int U, int C, int M>
+static void launch_plain(const Bsr3 &B, const T *val, const T *p, const T *b,
+                         T *y, double *part, const int *flag, double *dot_out,
+                         unsigned *counter, cudaStream_t st)
+{
+  static int grid = 0;  // per instantiation
+  if(!grid) grid = resident_grid(k_bsr_spmv<MODE, T, L, U, C, M>, 256, 0);
+  k_bsr_spmv<MODE, T, L, U, C, M><<<grid, 256, 0, st>>>(
+    B.nn, B.ptr.p, B.col.p, val, B.pstride, p, b, y, part, flag, dot_out, counter);
 }
 
 template <int MODE, typename T>
 static void launch_bsr(int variant, const Bsr3 &B, const T *val, const T *p,
                        const T *b, T *y, double *part, const int *flag,
-                       cudaStream_t st)
+                       cudaStream_t st, double *dot_out = nullptr,
+                       unsigned *counter = nullptr)
 {
-#define GB_BSR(L, U, C)                                                       \
-  k_bsr_spmv<MODE, T, L, U, C><<<kReduceBlocks, 256, 0, st>>>(               \
-    B.nn, B.ptr.p, B.col.p, val, B.pstride, p, b, y, part, flag)
+#define GB_BSR(L, U, C, M) \
+  launch_plain<MODE, T, L, U, C, M>(B, val, p, b, y, part, flag, dot_out, counter, st)
   switch(variant) {
-  case 6: launch_tma<MODE, T, 16>(B, val, p, b, y, part, flag, st); break;
-  case 7: launch_tma<MODE, T, 8>(B, val, p, b, y, part, flag, st); break;
-  case 1: GB_BSR(8, 2, 0); break;
-  case 2: GB_BSR(16, 2, 1); break;
-  case 3: GB_BSR(16, 2, 0); break;
-  case 4: GB_BSR(8, 4, 0); break;
-  case 5: GB_BSR(32, 2, 0); break;
-  default: GB_BSR(8, 2, 1); break;
+  case 6: launch_tma<MODE, T, 16>(B, val, p, b, y, part, flag, dot_out, counter, st); break;
+  case 7: launch_tma<MODE, T, 8>(B, val, p, b, y, part, flag, dot_out, counter, st); break;
+  case 1: GB_BSR(8, 2, 0, 0); break;
+  case 2: GB_BSR(16, 2, 1, 0); break;
+  case 3: GB_BSR(16, 2, 0, 0); break;
+  case 4: GB_BSR(8, 4, 0, 0); break;
+  case 5: GB_BSR(32, 2, 0, 0); break;
+  case 8: GB_BSR(8, 2, 0, 8); break;
+  case 9: GB_BSR(8, 4, 0, 4); break;
+  case 10: GB_BSR(8, 2, 0, 4); break;
+  default: GB_BSR(8, 2, 1, 0); break;
   }
 #undef GB_BSR
 }
 
 void bsr_spmv_dot32(const Bsr3 &B, const float *p, float *q, double *part,
-                    const int *flag, cudaStream_t st)
+                    const int *flag, double *dot_out, unsigned *counter,
+                    cudaStream_t st)
 {
-  launch_bsr<2, float>(B.var32, B, B.val32.p, p, nullptr, q, part, flag, st);
+  launch_bsr<2, float>(B.var32, B, B.val32.p, p, nullptr, q, part, flag, st,
+                       dot_out, counter);
 }
 void bsr_spmv_dot64(const Bsr3 &B, const double *p, double *q, double *part,
-                    const int *flag, cudaStream_t st)
+                    const int *flag, double *dot_out, unsigned *counter,
+                    cudaStream_t st)
 {
-  launch_bsr<2, double>(B.var64, B, B.val64.p, p, nullptr, q, part, flag, st);
+  launch_bsr<2, double>(B.var64, B, B.val64.p, p, nullptr, q, part, flag, st,
+                        dot_out, counter);
 }
 void bsr_residual64(const Bsr3 &B, const double *x, const double *b, double *r,
                     double *part, const int *flag, cudaStream_t st)
@@ -621,15 +676,43 @@ static int tune_one(Bsr3 &B, const T *val, int *out, cudaStream_t st)
   return GB300_OK;
 }
 
-int bsr_tune(gb300_matrix *A, Bsr3 &B, cudaStream_t st)
+// launch shapes already chosen, by (device, block rows, blocks, value size):
+// a matrix re-generated with the same structure is not tuned again
+static std::mutex g_tune_mutex;
+static std::map<std::tuple<int, int, long long, int>, int> g_tuned;
+
+template <typename T>
+static int tune_cached(Bsr3 &B, const T *val, int *out, cudaStream_t st)
+{
+  int dev = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  auto key = std::make_tuple(dev, B.nn, B.nblk, (int)sizeof(T));
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tuned.find(key);
+    if(it != g_tuned.end()) {
+      *out = it->second;
+      return GB300_OK;
+    }
+  }
+  GB_TRY(tune_one<T>(B, val, out, st));
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_tuned[key] = *out;
+  return GB300_OK;
+}
+
+int bsr_tune(gb300_matrix *A, Bsr3 &B, cudaStream_t st, bool tune64)
 {
   if(B.val32.p) {
-    if(A->bsr_var32 < 0) GB_TRY(tune_one<float>(B, B.val32.p, &A->bsr_var32, st));
+    if(A->bsr_var32 < 0) GB_TRY(tune_cached<float>(B, B.val32.p, &A->bsr_var32, st));
     B.var32 = A->bsr_var32;
   }
   if(B.val64.p) {
-    if(A->bsr_var64 < 0) GB_TRY(tune_one<double>(B, B.val64.p, &A->bsr_var64, st));
-    B.var64 = A->bsr_var64;
+    // FP64 products that only recompute a residual now and then keep the
+    // default shape; tuning them would cost more than it saves
+    if(A->bsr_var64 < 0 && tune64)
+      GB_TRY(tune_cached<double>(B, B.val64.p, &A->bsr_var64, st));
+    B.var64 = A->bsr_var64 < 0 ? 1 : A->bsr_var64;
   }
   return GB300_OK;
 }

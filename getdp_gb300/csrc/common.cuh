@@ -95,6 +95,35 @@ template <typename T, int NT> __device__ __forceinline__ T block_sum(T v)
   return s;
 }
 
+// Completion of a grid-wide reduction inside the kernel that produces the
+// partials: every block calls arrive_last after its partials are stored;
+// exactly one block, the last to arrive, gets true and then sees every
+// partial (read them with __ldcg).  It resets the counter for the next
+// launch.  Needs no co-residency and never waits.
+__device__ __forceinline__ bool arrive_last(unsigned *counter)
+{
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    unsigned t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x - 1);
+    if(last) *counter = 0u;
+  }
+  __syncthreads();
+  if(last) __threadfence();
+  return last != 0;
+}
+
+// the kReduceBlocks partials summed in the fixed order of the one-block
+// control kernels (NT threads), read through L2
+template <int NT> __device__ __forceinline__ double sum_partials_l2(const double *part)
+{
+  double s = 0.;
+  for(int i = threadIdx.x; i < kReduceBlocks; i += NT) s += __ldcg(part + i);
+  return block_sum<double, NT>(s);
+}
+
 // streaming loads for data read once per pass (matrix values and indices)
 template <typename T> __device__ __forceinline__ T ld_stream(const T *p)
 {

@@ -4,7 +4,8 @@
 //
 // Every scalar of a Krylov iteration (dot products, step lengths, the
 // stopping test of stopbis, iters.f:3275-3331) lives in device memory and is
-// computed by one-block control kernels, so iterations run back to back
+// computed on the device (one-block control kernels, or the last CTA of the
+// kernel that produced the partial sums), so iterations run back to back
 // without host round trips.  A fixed batch of iterations is captured once
 // in a CUDA graph and replayed; kernels after convergence see the device
 // flag `active == 0` and return at once.  The host reads one status word
@@ -90,6 +91,11 @@ struct CgState {
   int convert;   // r32 <- r64 pending
   int final_;    // the iteration cap was reached: last update then stop
   int updates;   // residual replacements done
+  // fused control: go = active && !update guards the iteration kernels;
+  // pq = <p, Ap> written by the SpMV's last CTA; arrival counters
+  int go;
+  double pq;
+  unsigned tick_dot, tick_step;
 };
 
 __global__ void k_cg_start(CgState *S, const double *__restrict__ part_rr,
@@ -108,84 +114,158 @@ __global__ void k_cg_start(CgState *S, const double *__restrict__ part_rr,
     S->status = 1;
     S->active = 1;
     S->alpha = S->beta = 0.;
+    S->update = S->convert = S->final_ = S->updates = 0;
+    S->tick_dot = S->tick_step = 0u;
     if(!(rr > 0.)) {  // zero right-hand side: x = 0 solves it
       S->active = 0;
       S->status = 0;
     }
+    S->go = S->active;
   }
 }
 
-__global__ void k_cg_alpha(CgState *S, const double *__restrict__ part_pq)
+// four consecutive entries through one 16-byte (float) or two 16-byte
+// (double) accesses; i4 indexes groups of four
+__device__ __forceinline__ void ld4(const float *p, long long i4, float (&v)[4])
 {
-  if(!S->active) return;
-  double pq = 0.;
-  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) pq += part_pq[i];
-  pq = block_sum<double, 256>(pq);
-  if(threadIdx.x == 0) {
-    S->its += 1;
-    // brkdn (iters.f:3368-3402)
-    bool bad = false;
-    if(pq > 0.) {
-      double b = 1. / pq;
-      if(!(b > 0.)) { bad = true; S->status = -9; }
-    }
-    else if(pq < 0.) {
-      double b = 1. / pq;
-      if(!(b < 0.)) { bad = true; S->status = -9; }
-    }
-    else if(pq == 0.) { bad = true; S->status = -3; }
-    else { bad = true; S->status = -9; }
-    if(bad) {
-      S->active = 0;
-      S->alpha = 0.;
-    }
-    else
-      S->alpha = S->rho / pq;
-  }
+  float4 t = reinterpret_cast<const float4 *>(p)[i4];
+  v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+}
+__device__ __forceinline__ void st4(float *p, long long i4, const float (&v)[4])
+{
+  reinterpret_cast<float4 *>(p)[i4] = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void ld4(const double *p, long long i4, double (&v)[4])
+{
+  double2 a = reinterpret_cast<const double2 *>(p)[2 * i4];
+  double2 b = reinterpret_cast<const double2 *>(p)[2 * i4 + 1];
+  v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+}
+__device__ __forceinline__ void st4(double *p, long long i4, const double (&v)[4])
+{
+  reinterpret_cast<double2 *>(p)[2 * i4] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2 *>(p)[2 * i4 + 1] = make_double2(v[2], v[3]);
 }
 
-template <typename T>
+// brkdn (iters.f:3368-3402) on <p, Ap>: 0, or the ipar(1) code
+__device__ __forceinline__ int cg_breakdown(double pq)
+{
+  if(pq > 0.) {
+    double b = 1. / pq;
+    return (b > 0.) ? 0 : -9;
+  }
+  if(pq < 0.) {
+    double b = 1. / pq;
+    return (b < 0.) ? 0 : -9;
+  }
+  if(pq == 0.) return -3;
+  return -9;
+}
+
+// the stopping test of the FP64 CG (stopbis: the iteration cap first, then
+// the residual test)
+__device__ void cg_check_tail(CgState *S, double rr)
+{
+  if(S->maxit > 0 && S->its >= S->maxit) {
+    S->status = -1;
+    S->active = 0;
+    S->res = sqrt(rr);
+    return;
+  }
+  S->res = sqrt(rr);
+  if(!(S->res > S->tol)) {
+    S->status = (S->res == S->res) ? 0 : -10;
+    S->active = 0;
+    return;
+  }
+  S->beta = S->res * S->res / S->rho;
+  S->rho = S->res * S->res;
+}
+
+// the reliable-update test of the mixed CG: replace the residual when the
+// FP32 one has dropped by delta since the last update, claims convergence,
+// or the iteration cap is reached
+__device__ void rcg_check_tail(CgState *S, double rr)
+{
+  S->convert = 0;
+  double tol2 = S->tol * S->tol;
+  bool cap = (S->maxit > 0 && S->its >= S->maxit);
+  if(cap || !(rr > tol2) || rr < S->delta2 * S->maxrr) {
+    S->update = 1;
+    S->final_ = cap ? 1 : 0;
+    S->res = sqrt(rr);
+    return;
+  }
+  S->update = 0;
+  if(rr > S->maxrr) S->maxrr = rr;
+  S->beta = rr / S->rho;
+  S->rho = rr;
+  S->res = sqrt(rr);
+}
+
+// One CG step after the SpMV: alpha = rho / <p, Ap> (from S->pq), x += alpha
+// p, r -= alpha Ap with the partials of ||r||^2; the last CTA then counts
+// the iteration, applies brkdn and the stopping (or update) test.
+template <typename T, bool MIXED>
 __global__ void __launch_bounds__(256)
-k_cg_update(int n, const CgState *__restrict__ S, T *__restrict__ x,
-            T *__restrict__ r, const T *__restrict__ p, const T *__restrict__ q,
-            double *__restrict__ part)
+k_cg_step(int n, CgState *__restrict__ S, T *__restrict__ x, T *__restrict__ r,
+          const T *__restrict__ p, const T *__restrict__ q, double *__restrict__ part)
 {
-  if(!S->active) return;
-  T a = (T)S->alpha;
+  if(!S->go) return;
+  const double pq = S->pq, rho = S->rho;
+  const int bad = cg_breakdown(pq);
   double v = 0.;
-  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-      i += (long long)gridDim.x * blockDim.x) {
-    x[i] += a * p[i];
-    T ri = r[i] - a * q[i];
-    r[i] = ri;
-    v += (double)ri * (double)ri;
+  if(!bad) {
+    // vectors are cudaMalloc'ed (256-byte aligned): groups of four, then
+    // the n % 4 remainder
+    T a = (T)(rho / pq);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long n4 = n / 4;
+    for(long long i4 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i4 < n4;
+        i4 += stride) {
+      T xv[4], rv[4], pv[4], qv[4];
+      ld4(x, i4, xv);
+      ld4(r, i4, rv);
+      ld4(p, i4, pv);
+      ld4(q, i4, qv);
+#pragma unroll
+      for(int c = 0; c < 4; c++) {
+        xv[c] += a * pv[c];
+        rv[c] = rv[c] - a * qv[c];
+        v += (double)rv[c] * (double)rv[c];
+      }
+      st4(x, i4, xv);
+      st4(r, i4, rv);
+    }
+    for(long long i = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        i < n; i += stride) {
+      x[i] += a * p[i];
+      T ri = r[i] - a * q[i];
+      r[i] = ri;
+      v += (double)ri * (double)ri;
+    }
   }
   double s = block_sum<double, 256>(v);
   if(threadIdx.x == 0) part[blockIdx.x] = s;
-}
-
-__global__ void k_cg_check(CgState *S, const double *__restrict__ part_rr)
-{
-  if(!S->active) return;
-  double rr = 0.;
-  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) rr += part_rr[i];
-  rr = block_sum<double, 256>(rr);
+  if(blockIdx.x == 0)
+    for(int b = gridDim.x + threadIdx.x; b < kReduceBlocks; b += blockDim.x) part[b] = 0.;
+  if(!arrive_last(&S->tick_step)) return;
+  double rr = sum_partials_l2<256>(part);
   if(threadIdx.x == 0) {
-    // stopbis: the iteration cap first, then the residual test
-    if(S->maxit > 0 && S->its >= S->maxit) {
-      S->status = -1;
+    S->its += 1;
+    if(bad) {
+      S->status = bad;
       S->active = 0;
-      S->res = sqrt(rr);
-      return;
+      S->alpha = 0.;
     }
-    S->res = sqrt(rr);
-    if(!(S->res > S->tol)) {
-      S->status = (S->res == S->res) ? 0 : -10;
-      S->active = 0;
-      return;
+    else {
+      S->alpha = rho / pq;
+      if(MIXED)
+        rcg_check_tail(S, rr);
+      else
+        cg_check_tail(S, rr);
     }
-    S->beta = S->res * S->res / S->rho;
-    S->rho = S->res * S->res;
+    S->go = S->active && !S->update;
   }
 }
 
@@ -193,10 +273,21 @@ template <typename T>
 __global__ void k_cg_p(int n, const CgState *__restrict__ S, T *__restrict__ p,
                        const T *__restrict__ r)
 {
-  if(!S->active) return;
+  if(!S->go) return;
   T b = (T)S->beta;
-  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-      i += (long long)gridDim.x * blockDim.x)
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long n4 = n / 4;
+  for(long long i4 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i4 < n4;
+      i4 += stride) {
+    T rv[4], pv[4];
+    ld4(r, i4, rv);
+    ld4(p, i4, pv);
+#pragma unroll
+    for(int c = 0; c < 4; c++) pv[c] = rv[c] + b * pv[c];
+    st4(p, i4, pv);
+  }
+  for(long long i = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+      i < n; i += stride)
     p[i] = r[i] + b * p[i];
 }
 
@@ -212,10 +303,9 @@ template <int TPR, typename V, typename XT>
 __global__ void __launch_bounds__(256)
 k_cg_spmv(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
           const V *__restrict__ val, const XT *__restrict__ p,
-          XT *__restrict__ q, double *__restrict__ part,
-          const CgState *__restrict__ S)
+          XT *__restrict__ q, double *__restrict__ part, CgState *S)
 {
-  if(!S->active) return;
+  if(!S->go) return;
   const int rows_per_block = 256 / TPR;
   int lane = threadIdx.x % TPR;
   int sub = threadIdx.x / TPR;
@@ -238,11 +328,15 @@ k_cg_spmv(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
   }
   double s = block_sum<double, 256>(red);
   if(threadIdx.x == 0) part[blockIdx.x] = s;
+  if(arrive_last(&S->tick_dot)) {
+    double d = sum_partials_l2<256>(part);
+    if(threadIdx.x == 0) S->pq = d;
+  }
 }
 
 template <typename V, typename XT>
 static void cg_spmv(const gb300_matrix *A, const V *val, const XT *p, XT *q,
-                    double *part, const CgState *S, cudaStream_t st)
+                    double *part, CgState *S, cudaStream_t st)
 {
   int n = A->n;
   switch(A->tpr) {
@@ -287,10 +381,8 @@ static int cg_core(cudaStream_t st, int n, SPMV spmv_dot, const T *rhs, T *y,
   GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   for(int it = 0; it < batch; it++) {
     spmv_dot(p, q, part, S, st);
-    k_cg_alpha<<<1, 256, 0, st>>>(S, part);
-    k_cg_update<T><<<kReduceBlocks, 256, 0, st>>>(n, S, y, r, p, q, part);
-    k_cg_check<<<1, 256, 0, st>>>(S, part);
-    k_cg_p<T><<<grid_for(n, 256, kReduceBlocks * 4), 256, 0, st>>>(n, S, p, r);
+    k_cg_step<T, false><<<kReduceBlocks, 256, 0, st>>>(n, S, y, r, p, q, part);
+    k_cg_p<T><<<grid_for((n + 3) / 4, 256, kReduceBlocks * 4), 256, 0, st>>>(n, S, p, r);
   }
   GB_CUDA(cudaStreamEndCapture(st, &graph));
   GB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
@@ -320,6 +412,7 @@ int bench_spmv(gb300_matrix *A, int precision, int reps, double *ms)
   CgState h;
   memset(&h, 0, sizeof(h));
   h.active = 1;
+  h.go = 1;
   CgState *S = (CgState *)W.state(sizeof(CgState));
   double *part = W.part();
   if(!S || !part) return GB300_ERR_CUDA;
@@ -331,7 +424,7 @@ int bench_spmv(gb300_matrix *A, int precision, int reps, double *ms)
   Bsr3 B;
   if(A->block3 &&
      bsr_build(A, A->val.p, precision == 0, precision != 0, B) == GB300_OK &&
-     bsr_tune(A, B, st) == GB300_OK) {
+     bsr_tune(A, B, st, precision == 0) == GB300_OK) {
     // the kernel the CG runs on a 3-component system: 3x3 blocks
     int n4 = 4 * B.nn;
     if(precision == 0) {
@@ -339,9 +432,11 @@ int bench_spmv(gb300_matrix *A, int precision, int reps, double *ms)
       double *q = (double *)W.vec(1, sizeof(double) * n4);
       if(!p || !q) return GB300_ERR_CUDA;
       k_copy<double><<<grid_for(n4, 256), 256, 0, st>>>(n4, B.val64.p, p);
-      for(int i = 0; i < 3; i++) bsr_spmv_dot64(B, p, q, part, &S->active, st);
+      for(int i = 0; i < 3; i++)
+        bsr_spmv_dot64(B, p, q, part, &S->go, &S->pq, &S->tick_dot, st);
       GB_CUDA(cudaEventRecord(e0, st));
-      for(int i = 0; i < reps; i++) bsr_spmv_dot64(B, p, q, part, &S->active, st);
+      for(int i = 0; i < reps; i++)
+        bsr_spmv_dot64(B, p, q, part, &S->go, &S->pq, &S->tick_dot, st);
       GB_CUDA(cudaEventRecord(e1, st));
     }
     else {
@@ -349,9 +444,11 @@ int bench_spmv(gb300_matrix *A, int precision, int reps, double *ms)
       float *q = (float *)W.vec(1, sizeof(float) * n4);
       if(!p || !q) return GB300_ERR_CUDA;
       k_copy<float><<<grid_for(n4, 256), 256, 0, st>>>(n4, B.val32.p, p);
-      for(int i = 0; i < 3; i++) bsr_spmv_dot32(B, p, q, part, &S->active, st);
+      for(int i = 0; i < 3; i++)
+        bsr_spmv_dot32(B, p, q, part, &S->go, &S->pq, &S->tick_dot, st);
       GB_CUDA(cudaEventRecord(e0, st));
-      for(int i = 0; i < reps; i++) bsr_spmv_dot32(B, p, q, part, &S->active, st);
+      for(int i = 0; i < reps; i++)
+        bsr_spmv_dot32(B, p, q, part, &S->go, &S->pq, &S->tick_dot, st);
       GB_CUDA(cudaEventRecord(e1, st));
     }
   }
@@ -415,34 +512,12 @@ __global__ void k_rcg_start(CgState *S, const double *__restrict__ part_rr,
     S->delta2 = delta * delta;
     S->update = S->convert = S->final_ = 0;
     S->updates = 0;
+    S->tick_dot = S->tick_step = 0u;
     if(!(rr > 0.)) {
       S->active = 0;
       S->status = 0;
     }
-  }
-}
-
-__global__ void k_rcg_check(CgState *S, const double *__restrict__ part_rr)
-{
-  if(!S->active) return;
-  double rr = 0.;
-  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) rr += part_rr[i];
-  rr = block_sum<double, 256>(rr);
-  if(threadIdx.x == 0) {
-    S->convert = 0;
-    double tol2 = S->tol * S->tol;
-    bool cap = (S->maxit > 0 && S->its >= S->maxit);
-    if(cap || !(rr > tol2) || rr < S->delta2 * S->maxrr) {
-      S->update = 1;
-      S->final_ = cap ? 1 : 0;
-      S->res = sqrt(rr);
-      return;
-    }
-    S->update = 0;
-    if(rr > S->maxrr) S->maxrr = rr;
-    S->beta = rr / S->rho;
-    S->rho = rr;
-    S->res = sqrt(rr);
+    S->go = S->active;
   }
 }
 
@@ -481,6 +556,7 @@ __global__ void k_rcg_after(CgState *S, const double *__restrict__ part_rr)
     S->rho = rr;
     S->maxrr = rr;
     S->convert = 1;
+    S->go = 1;
   }
 }
 
@@ -515,7 +591,7 @@ static int cg_mixed_core(cudaStream_t st, int n, SPMV32 spmv32, RES64 res64,
   double *part = W.part();
   if(!r32 || !p32 || !q32 || !x32 || !r64 || !S || !part) return GB300_ERR_CUDA;
   int gl = grid_for(n, 256);
-  int gs = grid_for(n, 256, kReduceBlocks * 4);
+  int gs = grid_for((n + 3) / 4, 256, kReduceBlocks * 4);
   GB_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), st));
   GB_CUDA(cudaMemsetAsync(x32, 0, n * sizeof(float), st));
   k_convert<float, double><<<gl, 256, 0, st>>>(n, rhs, r32);
@@ -524,36 +600,70 @@ static int cg_mixed_core(cudaStream_t st, int n, SPMV32 spmv32, RES64 res64,
   k_rcg_start<<<1, 256, 0, st>>>(S, part, rtol, maxit, 0.1);
   GB_CUDA(cudaGetLastError());
 
+  // Main graph: a batch of FP32 iterations (SpMV, step, direction).  When a
+  // step asks for a reliable update, go drops to 0 and the rest of the
+  // batch returns at once; the host then replays the update graph (fold the
+  // correction, FP64 residual, restart the FP32 residual, direction) and
+  // resumes.  The iterations and their arithmetic are those of the one-graph
+  // sequence; only the place where the update kernels run moves.
   const int batch = n > 200000 ? 16 : 32;
-  cudaGraph_t graph;
-  cudaGraphExec_t exec;
+  cudaGraph_t graph, ugraph;
+  cudaGraphExec_t exec, uexec;
   GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   for(int it = 0; it < batch; it++) {
     spmv32(p32, q32, part, S, st);
-    k_cg_alpha<<<1, 256, 0, st>>>(S, part);
-    k_cg_update<float><<<kReduceBlocks, 256, 0, st>>>(n, S, x32, r32, p32, q32, part);
-    k_rcg_check<<<1, 256, 0, st>>>(S, part);
-    // the reliable-update branch: kernels return at once unless S->update
-    // (about one step in 300), so they get the small fixed grid
-    k_rcg_fold<<<kReduceBlocks, 256, 0, st>>>(n, S, x, x32);
-    res64(x, rhs, r64, part, &S->update, st);
-    k_rcg_after<<<1, 256, 0, st>>>(S, part);
-    k_rcg_convert<<<kReduceBlocks, 256, 0, st>>>(n, S, r64, r32);
+    k_cg_step<float, true><<<kReduceBlocks, 256, 0, st>>>(n, S, x32, r32, p32, q32, part);
     k_cg_p<float><<<gs, 256, 0, st>>>(n, S, p32, r32);
   }
   GB_CUDA(cudaStreamEndCapture(st, &graph));
   GB_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-  int active = 1, launches = 0;
-  int max_launches = (maxit > 0 ? maxit / batch + 3 : 1 << 30);
-  while(active && launches < max_launches) {
-    GB_CUDA(cudaGraphLaunch(exec, st));
-    launches++;
-    GB_CUDA(cudaMemcpyAsync(&active, &S->active, sizeof(int),
+  GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  k_rcg_fold<<<kReduceBlocks, 256, 0, st>>>(n, S, x, x32);
+  res64(x, rhs, r64, part, &S->update, st);
+  k_rcg_after<<<1, 256, 0, st>>>(S, part);
+  k_rcg_convert<<<kReduceBlocks, 256, 0, st>>>(n, S, r64, r32);
+  k_cg_p<float><<<gs, 256, 0, st>>>(n, S, p32, r32);
+  GB_CUDA(cudaStreamEndCapture(st, &ugraph));
+  GB_CUDA(cudaGraphInstantiate(&uexec, ugraph, 0));
+  struct Flags {
+    int active, update;
+  } f = {1, 0};
+  long long launches = 0;
+  const long long max_launches =
+    maxit > 0 ? 2LL * (maxit / batch + 3) + 64 : (1LL << 40);
+  auto read_flags = [&]() -> int {
+    GB_CUDA(cudaMemcpyAsync(&f.active, &S->active, sizeof(int),
+                            cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemcpyAsync(&f.update, &S->update, sizeof(int),
                             cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
+    return GB300_OK;
+  };
+  int rc = GB300_OK;
+  while(f.active && launches < max_launches) {
+    if(cudaGraphLaunch(exec, st) != cudaSuccess) {
+      rc = GB300_ERR_CUDA;
+      break;
+    }
+    launches++;
+    if((rc = read_flags()) != GB300_OK) break;
+    if(f.active && f.update) {
+      if(cudaGraphLaunch(uexec, st) != cudaSuccess) {
+        rc = GB300_ERR_CUDA;
+        break;
+      }
+      if((rc = read_flags()) != GB300_OK) break;
+    }
   }
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);
+  cudaGraphExecDestroy(uexec);
+  cudaGraphDestroy(ugraph);
+  if(rc != GB300_OK) {
+    set_error("mixed CG: graph launch failed");
+    return rc;
+  }
+  int active = f.active;
   // anything not folded yet (a break-down stop) joins the FP64 solution
   k_fold_all<<<gl, 256, 0, st>>>(n, x, x32);
   GB_CUDA(cudaMemcpyAsync(hs, S, sizeof(CgState), cudaMemcpyDeviceToHost, st));
@@ -708,7 +818,7 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
     Bsr3 B;
     bool blocked = A->block3 &&
                    bsr_build(A, val, true, mixed, B) == GB300_OK &&
-                   bsr_tune(A, B, st) == GB300_OK;
+                   bsr_tune(A, B, st, !mixed) == GB300_OK;
     if(blocked) {
       // node-major 3x3 blocks: vectors of 4 entries per node
       int nn = B.nn, n4 = 4 * nn;
@@ -718,16 +828,16 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
       to_nodes64(nn, rhs, rhs4, st);
       if(!mixed) {
         auto spmv = [&](const double *pp, double *qq, double *part,
-                        const CgState *S, cudaStream_t s) {
-          bsr_spmv_dot64(B, pp, qq, part, &S->active, s);
+                        CgState *S, cudaStream_t s) {
+          bsr_spmv_dot64(B, pp, qq, part, &S->go, &S->pq, &S->tick_dot, s);
         };
         GB_TRY(cg_core<double>(st, n4, spmv, rhs4, x4, p->stopping_test,
                                p->nb_iter_max, &hs, W));
       }
       else {
         auto spmv = [&](const float *pp, float *qq, double *part,
-                        const CgState *S, cudaStream_t s) {
-          bsr_spmv_dot32(B, pp, qq, part, &S->active, s);
+                        CgState *S, cudaStream_t s) {
+          bsr_spmv_dot32(B, pp, qq, part, &S->go, &S->pq, &S->tick_dot, s);
         };
         auto res = [&](const double *xx, const double *bb, double *rr,
                        double *part, const int *flag, cudaStream_t s) {
@@ -740,7 +850,7 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
     }
     else if(!mixed) {
       auto spmv = [&](const double *pp, double *qq, double *part,
-                      const CgState *S, cudaStream_t s) {
+                      CgState *S, cudaStream_t s) {
         cg_spmv<double, double>(A, val, pp, qq, part, S, s);
       };
       GB_TRY(cg_core<double>(st, n, spmv, rhs, x, p->stopping_test,
@@ -752,7 +862,7 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
       k_convert<float, double><<<grid_for(A->nnz, 256), 256, 0, st>>>(A->nnz, val, v32.p);
       const float *v32p = v32.p;
       auto spmv = [&](const float *pp, float *qq, double *part,
-                      const CgState *S, cudaStream_t s) {
+                      CgState *S, cudaStream_t s) {
         cg_spmv<float, float>(A, v32p, pp, qq, part, S, s);
       };
       auto res = [&](const double *xx, const double *bb, double *rr,

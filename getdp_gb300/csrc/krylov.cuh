@@ -41,14 +41,19 @@ struct Bsr3 {
 };
 int bsr_build(const gb300_matrix *A, const double *val, bool want64,
               bool want32, Bsr3 &B);
-// pick the fastest SpMV launch shape for this matrix (cached in A)
-int bsr_tune(gb300_matrix *A, Bsr3 &B, cudaStream_t st);
+// pick the fastest SpMV launch shape for this matrix (cached in A and by
+// structure); the FP64 product is tuned only when tune64
+int bsr_tune(gb300_matrix *A, Bsr3 &B, cudaStream_t st, bool tune64);
 void to_nodes64(int nn, const double *in, double *out, cudaStream_t st);
 void from_nodes64(int nn, const double *in, double *out, cudaStream_t st);
+// q = A p with the partials of <p, q>; with dot_out, the last CTA also
+// writes the sum <p, q> there (counter: a zeroed word owned by the caller)
 void bsr_spmv_dot32(const Bsr3 &B, const float *p, float *q, double *part,
-                    const int *flag, cudaStream_t st);
+                    const int *flag, double *dot_out, unsigned *counter,
+                    cudaStream_t st);
 void bsr_spmv_dot64(const Bsr3 &B, const double *p, double *q, double *part,
-                    const int *flag, cudaStream_t st);
+                    const int *flag, double *dot_out, unsigned *counter,
+                    cudaStream_t st);
 void bsr_residual64(const Bsr3 &B, const double *x, const double *b, double *r,
                     double *part, const int *flag, cudaStream_t st);
 
