@@ -406,6 +406,7 @@ int gb300_matrix_destroy(gb300_matrix *A)
   if(!A) return GB300_OK;
   cudaStreamSynchronize(A->ctx->stream);
   if(A->ilu) ilu_free(A->ilu);
+  colour_free(A->mc);
   delete A;
   return GB300_OK;
 }
@@ -605,6 +606,7 @@ int gb300_matrix_set_csr(gb300_matrix *A, long long nnz, const int *rowptr,
   GB_CUDA(cudaStreamSynchronize(st));
   A->nnz = nnz;
   A->csr_valid = true;
+  A->pattern_version++;
   A->val32_valid = false;
   A->block3 = false;
   A->bsr_var32 = A->bsr_var64 = -1;

@@ -15,6 +15,7 @@
 namespace gb {
 
 struct ilu_data;
+struct Colouring;
 
 // last error message, per thread (read through gb300_last_error)
 void set_error(const char *fmt, ...);
@@ -219,4 +220,8 @@ struct gb300_matrix {
   int bsr_var32 = -1, bsr_var64 = -1;  // tuned SpMV launch shapes (-1: not yet)
   // ILU(0) state, created on demand by the solver
   gb::ilu_data *ilu = nullptr;
+  // bumped whenever the pattern is rebuilt; the multicolour ordering of the
+  // ILU solves (created on demand) remembers the version it was made for
+  unsigned pattern_version = 0;
+  gb::Colouring *mc = nullptr;
 };

@@ -882,8 +882,17 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
   }
   else if(p->algorithm == 8 || p->algorithm == 9 ||
           (p->algorithm == 1 && p->preconditioner == 6)) {
-    rc = gmres_solve(A, val, rhs, x, p, info, W);
-    if(rc != GB300_OK) return rc;
+    // Renumbering_Technique 1 (RCMK in Sparskit): this backend's own
+    // renumbering, a multicolour ordering, for the ILU(0) solves
+    bool used = false;
+    if(p->renumbering_technique == 1 && p->preconditioner == 6) {
+      rc = gmres_solve_coloured(A, val, rhs, x, p, info, W, &used);
+      if(rc != GB300_OK) return rc;
+    }
+    if(!used) {
+      rc = gmres_solve(A, val, rhs, x, p, info, W);
+      if(rc != GB300_OK) return rc;
+    }
   }
   else {
     set_error("Algorithm %d is not supported by this backend", p->algorithm);

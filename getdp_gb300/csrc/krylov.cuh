@@ -61,4 +61,17 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
                 double *x, const gb300_solver_params *p, gb300_solve_info *info,
                 Work &W);
 
+// multicolour ordering of a pattern for the ILU(0) solves (color.cu)
+struct Colouring {
+  int n = 0, ncolors = 0;
+  unsigned version = 0;        // pattern version it was built for
+  DevBuf<int> new_of, old_of;  // row permutation and its inverse
+  DevBuf<int> src;             // entry k of the permuted matrix = entry src[k] of A
+  gb300_matrix *B = nullptr;   // permuted structure (+ its ILU state)
+};
+void colour_free(Colouring *c);
+int gmres_solve_coloured(gb300_matrix *A, const double *val, const double *rhs,
+                         double *x, const gb300_solver_params *p,
+                         gb300_solve_info *info, Work &W, bool *used);
+
 }  // namespace gb

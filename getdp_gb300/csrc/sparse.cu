@@ -286,6 +286,7 @@ int build_pattern_from_elements(gb300_matrix *A, int ne, int nloc,
   GB_CUDA(cudaGetLastError());
   A->nnz = nnz;
   A->csr_valid = true;
+  A->pattern_version++;
   A->val32_valid = false;
   A->block3 = false;
   A->bsr_var32 = A->bsr_var64 = -1;
@@ -443,6 +444,7 @@ int build_csr_from_coo(gb300_matrix *A, long long m, const int *d_r,
   GB_CUDA(cudaStreamSynchronize(st));
   A->nnz = nnz;
   A->csr_valid = true;
+  A->pattern_version++;
   A->val32_valid = false;
   A->block3 = false;
   A->bsr_var32 = A->bsr_var64 = -1;
