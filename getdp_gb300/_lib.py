@@ -64,7 +64,7 @@ class TermBatch(ctypes.Structure):
                 ("elems", ctypes.c_void_p), ("elem_dofs", ctypes.c_void_p),
                 ("elem_sign", ctypes.c_void_p), ("coef", ctypes.c_void_p),
                 ("source", ctypes.c_void_p), ("coef2", ctypes.c_void_p),
-                ("p0", ctypes.c_double), ("p1", ctypes.c_double),
+                ("coef3", ctypes.c_void_p), ("p0", ctypes.c_double), ("p1", ctypes.c_double),
                 ("p2", ctypes.c_double), ("on_device", ctypes.c_int)]
 
 
@@ -111,6 +111,8 @@ SIGNATURES = {
     "gb300_generate_pattern": (_I, [_P, ctypes.POINTER(TermBatch)]),
     "gb300_generate_values": (_I, [_P, _P, ctypes.POINTER(TermBatch)]),
     "gb300_solve": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, ctypes.POINTER(SolveInfo)]),
+    "gb300_solve_batch": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, _I,
+                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(SolveInfo)]),
     "gb300_event_record": (_I, [_P, _I]),
     "gb300_event_elapsed": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_float)]),
     "gb300_bench_spmv": (_I, [_P, _I, _I, ctypes.POINTER(_D)]),

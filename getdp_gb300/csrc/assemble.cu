@@ -49,7 +49,8 @@ __global__ void __launch_bounds__(256)
 k_tri3(int ne, const double *__restrict__ nodes, const int *__restrict__ elems,
        const int *__restrict__ edofs, const double *__restrict__ nu,
        const double *__restrict__ js, const double *__restrict__ sigma,
-       double omega, CsrView A, double *__restrict__ b)
+       double omega, const double *__restrict__ omega_e, CsrView A,
+       double *__restrict__ b)
 {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if(e >= ne) return;
@@ -118,7 +119,7 @@ k_tri3(int ne, const double *__restrict__ nodes, const int *__restrict__ elems,
           scatter(A, d[i] + 1, d[j] + 1, K[i][j]);
         }
         if(sg != 0.) {
-          double w = M[i][j] * omega;
+          double w = M[i][j] * (omega_e ? omega_e[e] : omega);
           if(w != 0.) {
             scatter(A, d[i], d[j] + 1, -w);
             scatter(A, d[i] + 1, d[j], w);
@@ -404,12 +405,12 @@ k_tet4_curlcurl(int ne, const double *__restrict__ nodes,
 // host side
 // ---------------------------------------------------------------------------
 struct BatchDev {
-  DevBuf<double> nodes, coef, source, coef2;
+  DevBuf<double> nodes, coef, source, coef2, coef3;
   DevBuf<int> elems, edofs;
   DevBuf<signed char> esign;
   DevBuf<unsigned char> cflag;
   const double *p_nodes = nullptr, *p_coef = nullptr, *p_source = nullptr,
-               *p_coef2 = nullptr;
+               *p_coef2 = nullptr, *p_coef3 = nullptr;
   const int *p_elems = nullptr, *p_edofs = nullptr;
   const signed char *p_esign = nullptr;
 };
@@ -457,6 +458,7 @@ static int stage_batch(gb300_ctx *ctx, const gb300_term_batch *t, BatchDev &B,
     GB_TRY(stage(st, t->elem_sign, ne * nloc, t->on_device, B.esign, &B.p_esign));
     GB_TRY(stage(st, t->coef, ne, t->on_device, B.coef, &B.p_coef));
     GB_TRY(stage(st, t->source, ne, t->on_device, B.source, &B.p_source));
+    GB_TRY(stage(st, t->coef3, ne, t->on_device, B.coef3, &B.p_coef3));
   }
   GB_TRY(stage(st, t->coef2, ne, t->on_device, B.coef2, &B.p_coef2));
   return GB300_OK;
@@ -498,6 +500,7 @@ int generate_pattern(gb300_matrix *A, const gb300_term_batch *t)
   // the elasticity tables number unknowns component by component; the
   // solver checks the block structure itself before relying on it
   A->block3 = (t->kind == GB300_TERM_TET10_ELASTICITY);
+  A->block_rows = cplx ? 2 : 1;
   return GB300_OK;
 }
 
@@ -525,13 +528,13 @@ int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t)
       k_tri3<0><<<grid_for(ne, 256), 256, 0, st>>>(ne, B.p_nodes, B.p_elems,
                                                      B.p_edofs, B.p_coef,
                                                      B.p_source, nullptr, 0.,
-                                                     V, b->d.p);
+                                                     nullptr, V, b->d.p);
       break;
     case GB300_TERM_TRI3_EDDY_COMPLEX:
       k_tri3<1><<<grid_for(ne, 256), 256, 0, st>>>(ne, B.p_nodes, B.p_elems,
                                                      B.p_edofs, B.p_coef,
                                                      B.p_source, B.p_coef2,
-                                                     t->p0, V, b->d.p);
+                                                     t->p0, B.p_coef3, V, b->d.p);
       break;
     case GB300_TERM_TET10_ELASTICITY:
       k_tet10_elasticity<<<grid_for(ne, kElWarps), 32 * kElWarps, 0, st>>>(

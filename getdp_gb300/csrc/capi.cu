@@ -420,6 +420,7 @@ int gb300_matrix_reset(gb300_matrix *A)
   A->csr_valid = false;
   A->val32_valid = false;
   A->nnz = 0;
+  A->block_rows = 1;
   if(A->ilu) {
     ilu_free(A->ilu);
     A->ilu = nullptr;
@@ -444,6 +445,8 @@ int gb300_matrix_add_complex(gb300_matrix *A, double d1, double d2, int i,
                              int j, int k, int l)
 {
   GB_TRY(check(A, "matrix"));
+  // GetDP's complex unknowns are row pairs (2m, 2m + 1), k = i + 1
+  if(k == i + 1 && i % 2 == 0) A->block_rows = 2;
   if(d1) {
     GB_TRY(gb300_matrix_add_double(A, d1, i, j));
     GB_TRY(gb300_matrix_add_double(A, d1, k, l));
@@ -712,6 +715,20 @@ int gb300_solve(gb300_matrix *A, const gb300_vector *b,
   GB_TRY(check(x, "solution"));
   GB_TRY(gb300_matrix_assemble(A));
   return solve(A, b, p, x, info);
+}
+
+int gb300_solve_batch(gb300_matrix *A, const gb300_vector *b,
+                      const gb300_solver_params *p, gb300_vector *x, int nsys,
+                      const int *offsets, gb300_solve_info *infos)
+{
+  GB_TRY(check(A, "matrix"));
+  GB_TRY(check(b, "rhs"));
+  GB_TRY(check(p, "params"));
+  GB_TRY(check(x, "solution"));
+  GB_TRY(check(offsets, "offsets"));
+  GB_TRY(check(infos, "infos"));
+  GB_TRY(gb300_matrix_assemble(A));
+  return solve_batch(A, b, p, x, nsys, offsets, infos);
 }
 
 }  // extern "C"

@@ -224,4 +224,6 @@ struct gb300_matrix {
   // ILU solves (created on demand) remembers the version it was made for
   unsigned pattern_version = 0;
   gb::Colouring *mc = nullptr;
+  // rows per unknown (2: complex system in real form, harmonic-interleaved)
+  int block_rows = 1;
 };

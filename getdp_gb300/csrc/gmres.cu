@@ -330,7 +330,7 @@ __global__ void k_cvt(long long n, const TI *__restrict__ in, TO *__restrict__ o
 }
 
 // factor A's values (val) into the ILU(0) of the requested precision
-static int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out)
+int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out)
 {
   GB_TRY(ilu_setup(A));
   ilu_data *L = A->ilu;
@@ -365,8 +365,8 @@ static int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_r
 }
 
 // z = M^-1 v for the ILU(0) factor (double or float work precision)
-static void ilu_apply(const gb300_matrix *A, bool fp32, const double *v,
-                      double *z, float *t32, const int *flag, cudaStream_t st)
+void ilu_apply(const gb300_matrix *A, bool fp32, const double *v, double *z,
+               float *t32, const int *flag, cudaStream_t st)
 {
   const ilu_data *L = A->ilu;
   int n = A->n;
@@ -413,33 +413,6 @@ struct GmState {
   double cs[kMaxKrylov], sn[kMaxKrylov], g[kMaxKrylov + 1], y[kMaxKrylov];
   double h1[kMaxKrylov + 1], h2[kMaxKrylov + 1];
 };
-
-__device__ void givens_dev(double *x, double *y, double *c, double *s)
-{
-  if(*x == 0. && *y == 0.) {
-    *c = 1.;
-    *s = 0.;
-  }
-  else if(fabs(*y) > fabs(*x)) {
-    double t = *x / *y;
-    *x = sqrt(1. + t * t);
-    *s = copysign(1. / *x, *y);
-    *c = t * *s;
-  }
-  else if(fabs(*y) <= fabs(*x)) {
-    double t = *y / *x;
-    *y = sqrt(1. + t * t);
-    *c = copysign(1. / *y, *x);
-    *s = t * *c;
-  }
-  else {
-    *x = 0.;
-    *y = 0.;
-    *c = 1.;
-    *s = 0.;
-  }
-  *x = fabs(*x * *y);
-}
 
 // restart: r = rhs - A x was computed with its partial norms
 __global__ void k_gm_restart(GmState *S, const double *__restrict__ part, int m)

@@ -920,4 +920,113 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
   return rc;
 }
 
+// ---------------------------------------------------------------------------
+// independent systems held as the diagonal blocks of A: the batched form of
+// solve() (same scaling, renumbering and Krylov methods, one per block)
+// ---------------------------------------------------------------------------
+int solve_batch(gb300_matrix *A, const gb300_vector *bvec,
+                const gb300_solver_params *p, gb300_vector *xvec, int nsys,
+                const int *off, gb300_solve_info *infos)
+{
+  if(!A->csr_valid) {
+    set_error("matrix not assembled");
+    return GB300_ERR_ARG;
+  }
+  const int n = A->n;
+  if(bvec->n != n || xvec->n != n) {
+    set_error("vector sizes do not match the matrix");
+    return GB300_ERR_ARG;
+  }
+  if(nsys < 1 || !off || !infos || off[0] != 0 || off[nsys] != n) {
+    set_error("batched solve: offsets must run from 0 to the matrix size");
+    return GB300_ERR_ARG;
+  }
+  for(int q = 0; q < nsys; q++)
+    if(off[q + 1] < off[q]) {
+      set_error("batched solve: offsets must not decrease (system %d)", q);
+      return GB300_ERR_ARG;
+    }
+  if(n == 0) {
+    for(int q = 0; q < nsys; q++) memset(&infos[q], 0, sizeof(infos[q]));
+    return GB300_OK;
+  }
+  if(check_blocks(A, nsys, off) != GB300_OK) {
+    set_error("batched solve: an entry couples two systems");
+    return GB300_ERR_ARG;
+  }
+  cudaStream_t st = A->ctx->stream;
+  Work W;
+  {
+    std::vector<int> rp(n + 1);
+    GB_CUDA(cudaMemcpyAsync(rp.data(), A->rowptr.p, sizeof(int) * (n + 1),
+                            cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    for(int i = 0; i < n; i++)
+      if(rp[i + 1] - rp[i] <= 0) {
+        set_error("Zero row in matrix (row %d)", i + 1);
+        return GB300_ERR_ZERO_ROW;
+      }
+  }
+  const double *val = A->val.p;
+  const double *rhs = bvec->d.p;
+  DevBuf<double> sval, srhs, s;
+  bool scaled = false;
+  if(p->scaling == 1) {
+    DevBuf<int> zero;
+    GB_TRY(zero.alloc(1));
+    GB_TRY(s.alloc(n));
+    GB_CUDA(cudaMemsetAsync(zero.p, 0, sizeof(int), st));
+    k_diag_scal<<<grid_for(n, 256), 256, 0, st>>>(n, A->rowptr.p, A->col.p, A->val.p,
+                                                   s.p, zero.p);
+    int hz = 0;
+    GB_CUDA(cudaMemcpyAsync(&hz, zero.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if(!hz) {
+      GB_TRY(sval.alloc(A->nnz));
+      GB_TRY(srhs.alloc(n));
+      k_scale_vals<<<grid_for(n, 8), 256, 0, st>>>(n, A->rowptr.p, A->col.p, A->val.p,
+                                                    s.p, sval.p);
+      k_mul<<<grid_for(n, 256), 256, 0, st>>>(n, bvec->d.p, s.p, srhs.p);
+      val = sval.p;
+      rhs = srhs.p;
+      scaled = true;
+    }
+  }
+  double *x = xvec->d.p;
+  bool coloured = false;
+  if(p->renumbering_technique == 1 && p->preconditioner == 6) {
+    int rc = colour_build(A, nsys, off);
+    if(rc != GB300_OK && rc != GB300_ERR_UNSUPPORTED) return rc;
+    coloured = (rc == GB300_OK);
+  }
+  if(coloured) {
+    Colouring *C = A->mc;
+    gb300_matrix *B = C->B;
+    DevBuf<double> rb, yb;
+    GB_TRY(rb.alloc(n));
+    GB_TRY(yb.alloc(n));
+    permute_system(C, A->nnz, val, rhs, B->val.p, rb.p, st);
+    GB_TRY(gmres_solve_batch(B, B->val.p, rb.p, yb.p, p, nsys, off, infos, W));
+    unpermute_solution(C, yb.p, x, st);
+  }
+  else
+    GB_TRY(gmres_solve_batch(A, val, rhs, x, p, nsys, off, infos, W));
+  if(scaled) k_mul<<<grid_for(n, 256), 256, 0, st>>>(n, x, s.p, x);
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(st));
+  int failed = 0, first = -1;
+  for(int q = 0; q < nsys; q++)
+    if(infos[q].status != 0) {
+      failed++;
+      if(first < 0) first = q;
+    }
+  if(failed) {
+    set_error("Iterative solver terminated in %d of %d systems (first: system %d, "
+              "code = %d after %d iterations)",
+              failed, nsys, first, infos[first].status, infos[first].iterations);
+    return GB300_ERR_SOLVER;
+  }
+  return GB300_OK;
+}
+
 }  // namespace gb

@@ -57,19 +57,67 @@ void bsr_spmv_dot64(const Bsr3 &B, const double *p, double *q, double *part,
 void bsr_residual64(const Bsr3 &B, const double *x, const double *b, double *r,
                     double *part, const int *flag, cudaStream_t st);
 
+// ILU(0) of A's pattern on the values val (FP64, or FP32 storage), and its
+// application z = M^-1 v guarded by *flag (gmres.cu)
+int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out);
+void ilu_apply(const gb300_matrix *A, bool fp32, const double *v, double *z,
+               float *t32, const int *flag, cudaStream_t st);
+
+// the Givens rotation of iters.f's givens (3235-3273): zeroes y against x;
+// x becomes the norm, (c, s) the rotation
+__device__ inline void givens_dev(double *x, double *y, double *c, double *s)
+{
+  if(*x == 0. && *y == 0.) {
+    *c = 1.;
+    *s = 0.;
+  }
+  else if(fabs(*y) > fabs(*x)) {
+    double t = *x / *y;
+    *x = sqrt(1. + t * t);
+    *s = copysign(1. / *x, *y);
+    *c = t * *s;
+  }
+  else if(fabs(*y) <= fabs(*x)) {
+    double t = *y / *x;
+    *y = sqrt(1. + t * t);
+    *c = copysign(1. / *y, *x);
+    *s = t * *c;
+  }
+  else {
+    *x = 0.;
+    *y = 0.;
+    *c = 1.;
+    *s = 0.;
+  }
+  *x = fabs(*x * *y);
+}
+
 int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
                 double *x, const gb300_solver_params *p, gb300_solve_info *info,
                 Work &W);
+
+// batched GMRES/FGMRES over the diagonal blocks off[0..nsys] of A
+// (gmres_batch.cu); infos[p] per system
+int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
+                      double *x, const gb300_solver_params *p, int nsys,
+                      const int *off, gb300_solve_info *infos, Work &W);
+int check_blocks(const gb300_matrix *A, int nsys, const int *off);
 
 // multicolour ordering of a pattern for the ILU(0) solves (color.cu)
 struct Colouring {
   int n = 0, ncolors = 0;
   unsigned version = 0;        // pattern version it was built for
+  std::vector<int> seg;        // diagonal blocks it was built for
+  int bs = 1;                  // rows per coloured vertex
   DevBuf<int> new_of, old_of;  // row permutation and its inverse
   DevBuf<int> src;             // entry k of the permuted matrix = entry src[k] of A
   gb300_matrix *B = nullptr;   // permuted structure (+ its ILU state)
 };
 void colour_free(Colouring *c);
+int colour_build(gb300_matrix *A, int nseg, const int *off);
+void permute_system(const Colouring *C, long long nnz, const double *val,
+                    const double *rhs, double *bval, double *brhs, cudaStream_t st);
+void unpermute_solution(const Colouring *C, const double *y, double *x, cudaStream_t st);
 int gmres_solve_coloured(gb300_matrix *A, const double *val, const double *rhs,
                          double *x, const gb300_solver_params *p,
                          gb300_solve_info *info, Work &W, bool *used);

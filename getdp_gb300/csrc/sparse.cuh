@@ -42,5 +42,7 @@ void ilu_free(ilu_data *d);
 
 int solve(gb300_matrix *A, const gb300_vector *b, const gb300_solver_params *p,
           gb300_vector *x, gb300_solve_info *info);
+int solve_batch(gb300_matrix *A, const gb300_vector *b, const gb300_solver_params *p,
+                gb300_vector *x, int nsys, const int *off, gb300_solve_info *infos);
 
 }  // namespace gb

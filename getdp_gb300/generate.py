@@ -37,7 +37,10 @@ def term_arrays(p: Problem, dm: DofMap) -> dict:
         kind = _lib.TERM_TRI3_EDDY_COMPLEX
         a["source"] = np.ascontiguousarray(p.source, np.float64)
         a["coef2"] = np.ascontiguousarray(p.params["sigma"], np.float64)
-        p0 = p.params["freq"] * TWO_PI
+        if "omega_e" in p.params:  # a batch: each problem's own frequency
+            a["coef3"] = np.ascontiguousarray(p.params["omega_e"], np.float64)
+        else:
+            p0 = p.params["freq"] * TWO_PI
     elif f == "elasticity":
         kind = _lib.TERM_TET10_ELASTICITY
         p0 = p.params["poisson"]
@@ -60,7 +63,8 @@ def _batch(arrays: dict, ptrs: dict, on_device: int) -> TermBatch:
     t.kind = arrays["_kind"]
     t.n_nodes = arrays["nodes"].shape[0]
     t.n_elems = arrays["elems"].shape[0]
-    for k in ("nodes", "elems", "elem_dofs", "elem_sign", "coef", "source", "coef2"):
+    for k in ("nodes", "elems", "elem_dofs", "elem_sign", "coef", "source", "coef2",
+              "coef3"):
         setattr(t, k, ptrs.get(k))
     t.p0, t.p1, t.p2 = arrays["_p"]
     t.on_device = on_device

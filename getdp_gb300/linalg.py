@@ -311,6 +311,29 @@ def LinAlg_Solve(A: gMatrix, B: gVector, Solver: gSolver, X: gVector,
     return d
 
 
+def LinAlg_SolveBatch(A: gMatrix, B: gVector, Solver: gSolver, X: gVector,
+                      offsets) -> list:
+    """LinAlg_Solve over independent systems held as A's diagonal blocks
+    (system k: rows offsets[k]..offsets[k+1]); one information dict per
+    system.  A system that fails only warns, as LinAlg_Solve does."""
+    B._flush()
+    off = np.ascontiguousarray(offsets, np.int32)
+    nsys = len(off) - 1
+    infos = (SolveInfo * max(nsys, 1))()
+    rc = _lib.load().gb300_solve_batch(
+        A.h, B.h, ctypes.byref(Solver.params), X.h, nsys,
+        off.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), infos)
+    if rc != 0 and rc != 4:
+        check(rc)
+    out = [infos[k].as_dict() for k in range(nsys)]
+    if rc == 4:
+        msg = _lib.load().gb300_last_error().decode()
+        for d in out:
+            if d["status"] != 0:
+                d["warning"] = msg
+    return out
+
+
 def LinAlg_SolveAgain(A: gMatrix, B: gVector, Solver: gSolver, X: gVector,
                       solverIndex: int = 0) -> dict:
     return LinAlg_Solve(A, B, Solver, X, solverIndex)

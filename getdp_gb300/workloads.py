@@ -396,6 +396,73 @@ def dofmap_for(p: Problem) -> DofMap:
 
 
 # --------------------------------------------------------------------------
+# batches of independent problems (frequency / material sweeps)
+# --------------------------------------------------------------------------
+
+def eddy_sweep(n_problems: int = 512, seed: int = 7, n_min: int = 32,
+               n_max: int = 160) -> list:
+    """Independent complex eddy-current problems of uneven size: side n
+    drawn uniformly from {n_min..n_max} cells, and per problem its own
+    seeded jitter, 1-4 conductor disks and log-uniform frequency in
+    [10 Hz, 10 kHz] (eddy_2d)."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(n_min, n_max + 1, size=n_problems)
+    return [eddy_2d(int(n), seed=int(seed * 100003 + k)) for k, n in enumerate(sizes)]
+
+
+@dataclasses.dataclass
+class Batch:
+    """Independent problems as one system with diagonal blocks: problem k
+    owns unknowns offsets[k]..offsets[k+1] (its own GetDP numbering shifted
+    by offsets[k]) and nodes node_offsets[k]..node_offsets[k+1]."""
+
+    problem: Problem
+    dofmap: DofMap
+    offsets: np.ndarray
+    node_offsets: np.ndarray
+    parts: list
+    dofmaps: list
+
+
+def concat_problems(problems: list) -> Batch:
+    """One Problem / DofMap holding every problem's elements, for a single
+    batched Generate; the per-element angular frequency (params['omega_e'])
+    carries each problem's own frequency."""
+    f = problems[0].formulation
+    if any(p.formulation != f for p in problems):
+        raise ValueError("a batch holds problems of one formulation")
+    dms = [dofmap_for(p) for p in problems]
+    off = np.zeros(len(problems) + 1, np.int64)
+    noff = np.zeros(len(problems) + 1, np.int64)
+    for k, (p, dm) in enumerate(zip(problems, dms)):
+        off[k + 1] = off[k] + dm.n_dof
+        noff[k + 1] = noff[k] + p.mesh.n_nodes
+    if off[-1] >= 2 ** 31:
+        raise ValueError("batch too large for 32-bit unknown numbers")
+    nodes = np.concatenate([p.mesh.nodes for p in problems])
+    elems = np.concatenate([p.mesh.elems + noff[k] for k, p in enumerate(problems)])
+    edofs = np.concatenate([np.where(dm.elem_dofs >= 0, dm.elem_dofs + off[k], -1)
+                            for k, dm in enumerate(dms)]).astype(np.int32)
+    esign = np.concatenate([dm.elem_sign for dm in dms])
+    region = np.concatenate([p.mesh.region for p in problems])
+    mesh = Mesh(nodes, problems[0].mesh.kind, elems.astype(np.int32), region,
+                problems[0].mesh.bnd_kind, np.zeros((0, problems[0].mesh.bnd.shape[1]), np.int32),
+                np.zeros(0, np.int32))
+    params = {}
+    if f == "eddy2d":
+        params["sigma"] = np.concatenate([p.params["sigma"] for p in problems])
+        params["omega_e"] = np.concatenate(
+            [np.full(p.mesh.n_elems, p.params["freq"] * 6.2831853071795865)
+             for p in problems])
+        params["freq"] = float("nan")
+    prob = Problem(f"batch_{f}_{len(problems)}", mesh, f,
+                   np.concatenate([p.coef for p in problems]),
+                   np.concatenate([p.source for p in problems]), params)
+    dm = DofMap(int(off[-1]), edofs, esign, dms[0].ncomp, dms[0].nharm)
+    return Batch(prob, dm, off.astype(np.int32), noff, problems, dms)
+
+
+# --------------------------------------------------------------------------
 # GetDP input files (used to run the reference on the same problem)
 # --------------------------------------------------------------------------
 

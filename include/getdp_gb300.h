@@ -195,6 +195,9 @@ typedef struct gb300_term_batch {
   const double *coef;            /* per element */
   const double *source;          /* per element, or NULL */
   const double *coef2;           /* per element, or NULL */
+  const double *coef3;           /* per element, or NULL: TRI3_EDDY_COMPLEX
+                                    angular frequency (overrides p0), so one
+                                    batch can carry a frequency sweep */
   double p0, p1, p2;
   int on_device;                 /* 1: the arrays above are device pointers */
 } gb300_term_batch;
@@ -242,6 +245,19 @@ int gb300_residual_noalloc(gb300_matrix *A, const gb300_vector *x,
 int gb300_solve(gb300_matrix *A, const gb300_vector *b,
                 const gb300_solver_params *p, gb300_vector *x,
                 gb300_solve_info *info);
+
+/* Batched LinAlg_Solve (Sparskit.cpp:108-634 once per system): the nsys
+   independent systems are the diagonal blocks of A, system k owning rows
+   [offsets[k], offsets[k+1]) (offsets[0] = 0, offsets[nsys] = n, host
+   array); an entry coupling two blocks is an error.  Each system is solved
+   as gb300_solve would solve it alone (GMRES or FGMRES, Preconditioner 0 or
+   6; Renumbering_Technique 1 reorders within each block), with its own
+   convergence test, iteration count and status in infos[k] (nsys entries);
+   all of them share every kernel launch.  Returns GB300_ERR_SOLVER (with
+   the solutions and infos filled) if any system did not converge. */
+int gb300_solve_batch(gb300_matrix *A, const gb300_vector *b,
+                      const gb300_solver_params *p, gb300_vector *x, int nsys,
+                      const int *offsets, gb300_solve_info *infos);
 
 #ifdef __cplusplus
 }
