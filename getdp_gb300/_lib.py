@@ -111,6 +111,8 @@ SIGNATURES = {
     "gb300_generate_pattern": (_I, [_P, ctypes.POINTER(TermBatch)]),
     "gb300_generate_values": (_I, [_P, _P, ctypes.POINTER(TermBatch)]),
     "gb300_solve": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, ctypes.POINTER(SolveInfo)]),
+    "gb300_post_elements": (_I, [ctypes.POINTER(TermBatch), _P, _P]),
+    "gb300_post_points": (_I, [ctypes.POINTER(TermBatch), _P, _I, _P, _P, _P, _P]),
     "gb300_solve_batch": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, _I,
                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(SolveInfo)]),
     "gb300_event_record": (_I, [_P, _I]),

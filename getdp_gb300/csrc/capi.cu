@@ -717,6 +717,24 @@ int gb300_solve(gb300_matrix *A, const gb300_vector *b,
   return solve(A, b, p, x, info);
 }
 
+int gb300_post_elements(const gb300_term_batch *t, const gb300_vector *x,
+                        double *out)
+{
+  GB_TRY(check(t, "term batch"));
+  GB_TRY(check(x, "solution"));
+  GB_TRY(check(out, "out"));
+  return post_elements(t, x, out);
+}
+
+int gb300_post_points(const gb300_term_batch *t, const gb300_vector *x, int npts,
+                      const double *xyz, double *field, double *curl, int *elem)
+{
+  GB_TRY(check(t, "term batch"));
+  GB_TRY(check(x, "solution"));
+  if(npts > 0) GB_TRY(check(xyz, "xyz"));
+  return post_points(t, x, npts, xyz, field, curl, elem);
+}
+
 int gb300_solve_batch(gb300_matrix *A, const gb300_vector *b,
                       const gb300_solver_params *p, gb300_vector *x, int nsys,
                       const int *offsets, gb300_solve_info *infos)

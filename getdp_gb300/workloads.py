@@ -637,6 +637,33 @@ Resolution {{ {{ Name R; System {{ {{ Name A; NameOfFormulation F; }} }}
     raise ValueError(f)
 
 
+def post_text(p: Problem, points) -> str:
+    """PostProcessing / PostOperation blocks for pro_text(p): the field and
+    its curl printed on every element (Format Table, file post_elem.txt) and
+    the field at each of `points` (file post_pts.txt)."""
+    f = p.formulation
+    if f not in ("magnetostatics2d", "eddy2d", "curlcurl"):
+        raise ValueError(f)
+    dom = "Dom"
+    quants = (f"{{ Name av; Value {{ Local {{ [ {{a}} ]; In {dom}; Jacobian Vol; }} }} }}\n"
+              f"    {{ Name b; Value {{ Local {{ [ {{d a}} ]; In {dom}; Jacobian Vol; }} }} }}")
+    ops = [f'Print[ b, OnElementsOf {dom}, Format Table, File "post_elem.txt" ];']
+    for (x, y, z) in points:
+        ops.append(f'Print[ av, OnPoint {{{x:.17g}, {y:.17g}, {z:.17g}}}, Format Table, '
+                   f'File > "post_pts.txt" ];')
+        ops.append(f'Print[ b, OnPoint {{{x:.17g}, {y:.17g}, {z:.17g}}}, Format Table, '
+                   f'File > "post_pts_b.txt" ];')
+    return f"""PostProcessing {{ {{ Name P; NameOfFormulation F;
+  Quantity {{
+    {quants}
+  }} }} }}
+PostOperation {{ {{ Name Map; NameOfPostProcessing P;
+  Operation {{
+    {chr(10).join('    ' + o for o in ops)}
+  }} }} }}
+"""
+
+
 def write_pro(p: Problem, path: str) -> None:
     """Write the problem file; elasticity needs one region per element."""
     if p.formulation == "elasticity":

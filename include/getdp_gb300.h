@@ -211,6 +211,25 @@ int gb300_generate_pattern(gb300_matrix *A, const gb300_term_batch *t);
 int gb300_generate_values(gb300_matrix *A, gb300_vector *b,
                           const gb300_term_batch *t);
 
+/* ---- post-processing ------------------------------------------------- */
+/* PostOperation Print[ {d a}, OnElementsOf ... ] (Pos_Print.cpp,
+   Pos_FemInterpolation.cpp, Cal_PostQuantity.cpp): the curl of the solution
+   x on every element of the term batch t, for the formulations
+   TRI3_MAGNETOSTATIC, TRI3_EDDY_COMPLEX and TET4_EDGE_CURLCURL (fixed
+   unknowns are zero), into the host array out: 2D (bx, by) per element and
+   harmonic (2 or 4 values per element), 3D (bx, by, bz). */
+int gb300_post_elements(const gb300_term_batch *t, const gb300_vector *x,
+                        double *out);
+/* Print[ {a}, OnPoint {x,y,z} ] and Print[ {d a}, OnPoint ... ] (the point
+   located as Pos_Search.cpp does) for npts points given as host xyz triples:
+   field receives a_z per harmonic (2D: 1 or 2 values per point) or the
+   vector a (3D, 3 values); curl as gb300_post_elements; elem the 0-based
+   element holding the point, or -1 outside the mesh (values 0).  A point on
+   a face shared by several elements takes the lowest-numbered one.  NULL
+   outputs are skipped. */
+int gb300_post_points(const gb300_term_batch *t, const gb300_vector *x, int npts,
+                      const double *xyz, double *field, double *curl, int *elem);
+
 /* ---- measurement ---------------------------------------------------- */
 /* CUDA events on the context's stream (slots 0..15), for timing calls
    made through this library on the device. */

@@ -12,8 +12,10 @@ _GEN = {"ms2d": W.magnetostatics_2d, "el": W.elasticity_p2,
 
 
 def names():
+    """The solve fixtures (post-processing fixtures are post_*.npz)."""
     return sorted(os.path.basename(f)[:-4]
-                  for f in glob.glob(os.path.join(GOLDEN, "*.npz")))
+                  for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(f).startswith("post_"))
 
 
 def load(name):
