@@ -53,13 +53,16 @@ def parse():
     ap.add_argument("--n", type=int, default=None,
                     help="cells per side (default: the workload's own size)")
     ap.add_argument("--workload", default="elasticity",
-                    choices=["elasticity", "magnetostatics2d", "curlcurl", "eddysweep"],
+                    choices=["elasticity", "magnetostatics2d", "curlcurl", "eddysweep",
+                             "nonlinear"],
                     help="elasticity: 3D P2 elasticity, Jacobi-CG (the headline); "
                          "magnetostatics2d: 2D P1 a_z, ILU(0)-GMRES(50) to 1e-10; "
                          "curlcurl: 3D Whitney-edge curl-curl, ILU(0)-FGMRES(40) "
                          "to 1e-8, FP64 and FP32-ILU; eddysweep: 512 complex 2D "
                          "eddy-current problems of 32^2..160^2 cells in one batched "
                          "Generate + batched ILU(0)-GMRES")
+    ap.add_argument("--cpu-n", type=int, default=128,
+                    help="nonlinear: mesh size of the CPU (oracle) comparison run")
     ap.add_argument("--problems", type=int, default=512,
                     help="eddysweep: number of problems")
     ap.add_argument("--skip-cpu", action="store_true")
@@ -500,9 +503,105 @@ def run_sweep(args, ws, rank, local):
         print(json.dumps(line))
 
 
+# adaptive relaxation factors of the Newton step (SolveJac_AdaptRelax list)
+RELAX = (1.0, 0.5, 0.25, 0.125, 0.0625, 0.03125)
+
+
+def run_nonlinear(args, ws, rank, local):
+    """Nonlinear 2D magnetostatics (saturating B-H law, lognormal field):
+    the reference's Newton loop (Generate; Solve; Generate; GetResidual;
+    While[...] { Solve; Generate; GetResidual }) with adaptive relaxation of
+    each step, to a 1e-8 relative nonlinear residual, each Solve
+    ILU(0)-GMRES(50) to 1e-10 (FP64), or FGMRES with an FP32 ILU(0); wall
+    time of the whole loop."""
+    from getdp_gb300 import _lib
+    from getdp_gb300 import generate as G
+    from getdp_gb300 import linalg as LA
+    from getdp_gb300 import nonlinear as NL
+    from getdp_gb300 import workloads as W
+    _lib.load(build_if_missing=True)
+    LA.context()
+    n = args.n or 1024
+
+    def params(prec):
+        S = LA.LinAlg_CreateSolver(None)
+        for k, v in dict(Algorithm=8 if prec == 0 else 9, Preconditioner=6, Krylov_Size=50,
+                         Stopping_Test=1e-10, Nb_Iter_Max=20000, Renumbering_Technique=1,
+                         Precision=prec).items():
+            S.set(k, v)
+        S["stopping_test"] = 1e-10
+        return S
+
+    def run_gpu(size, prec, reps):
+        p = W.nonlinear_2d(n=size, seed=5)
+        dm = W.dofmap_for(p)
+        terms = G.DeviceTerms(p, dm)
+        out = None
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            r = NL.newton(terms, dm.n_dof, params(prec), tol_rel=1e-8, iter_max=50,
+                          relaxation=RELAX)
+            ts.append(time.perf_counter() - t0)
+            out = r
+        return {"s": float(np.median(ts)), "newton_steps": len(out.history) - 1,
+                "linear_iterations": int(sum(s["iterations"] for s in out.solves)),
+                "final_rel_residual": out.history[-1] / out.history[0],
+                "converged": out.converged, "unknowns": dm.n_dof}, out
+
+    res = {}
+    for prec in (0, 1):
+        run_gpu(n, prec, 1)  # warm-up (pattern, colouring, tuning)
+        res[prec], _ = run_gpu(n, prec, max(args.steps, 1))
+    best = min(res.values(), key=lambda r: r["s"])
+    line = {"metric": "nonlinear 2D magnetostatics: time to 1e-8 Newton residual "
+                      "(Generate + Solve per step)",
+            "value": best["s"], "unit": "s", "n_gpus": ws, "steps": args.steps,
+            "warmup": 1, "ms_per_step": best["s"] * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"nonlinear a_z P1 {n}^2x2 triangles, lognormal GRF "
+                                   "reluctivity x saturating B-H law, 8 current blobs; "
+                                   "Newton, ILU(0)-(F)GMRES(50) per step",
+                       "elements": 2 * n * n, "unknowns": res[0]["unknowns"],
+                       "parallelism": f"replicas x{ws}"},
+            "fp64": res[0], "mixed": res[1]}
+    if not args.skip_cpu and rank == 0:
+        import oracle
+        oracle.build()
+        m = args.cpu_n
+        p = W.nonlinear_2d(n=m, seed=5)
+        dm = W.dofmap_for(p)
+        t0 = time.perf_counter()
+        xo, hist, its = oracle.newton(p, dm, tol=1e-8, iter_max=50, relaxation=RELAX,
+                                      algorithm=8,
+                                      preconditioner=6, renumbering=1, krylov_size=50,
+                                      stopping_test=float(np.float32(1e-10)),
+                                      nb_iter_max=20000)
+        t_cpu = time.perf_counter() - t0
+        gsame, gout = run_gpu(m, 0, 1)
+        err = float(np.linalg.norm(gout.x.numpy() - xo) / np.linalg.norm(xo))
+        line["cpu_baseline"] = {
+            "value": t_cpu, "unit": "s", "cores": 1, "kind": "port",
+            "sample": json.dumps({"size": f"{m}^2", "newton_steps": len(hist) - 1,
+                                  "linear_iterations": int(sum(its)),
+                                  "gpu_fp64_same_size_s": round(gsame["s"], 4),
+                                  "gpu_newton_steps_same_size": gsame["newton_steps"],
+                                  "rel_diff_solution_vs_oracle": err})}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     args = parse()
     ws, rank, local, pg = dist_setup(args)
+    if args.workload == "nonlinear":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference arm times the headline workload only"}))
+            return
+        run_nonlinear(args, ws, rank, local)
+        return
     if args.workload == "eddysweep":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":

@@ -20,6 +20,7 @@ TERM_TRI3_MAGNETOSTATIC = 1
 TERM_TRI3_EDDY_COMPLEX = 2
 TERM_TET10_ELASTICITY = 3
 TERM_TET4_EDGE_CURLCURL = 4
+TERM_TRI3_MAGNETOSTATIC_NL = 5
 
 
 class GetDPError(RuntimeError):
@@ -94,6 +95,7 @@ SIGNATURES = {
     "gb300_vector_get": (_I, [_P, _P]),
     "gb300_vector_size": (_I, [_P, ctypes.POINTER(_I)]),
     "gb300_vector_norm2": (_I, [_P, ctypes.POINTER(_D)]),
+    "gb300_vector_axpby": (_I, [_D, _P, _D, _P]),
     "gb300_vector_add_values": (_I, [_P, _I, _P, _P]),
     "gb300_matrix_create": (_I, [_P, _I, _PP]),
     "gb300_matrix_destroy": (_I, [_P]),
@@ -110,6 +112,7 @@ SIGNATURES = {
     "gb300_matrix_mult": (_I, [_P, _P, _P]),
     "gb300_generate_pattern": (_I, [_P, ctypes.POINTER(TermBatch)]),
     "gb300_generate_values": (_I, [_P, _P, ctypes.POINTER(TermBatch)]),
+    "gb300_generate_values_at": (_I, [_P, _P, ctypes.POINTER(TermBatch), _P]),
     "gb300_solve": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, ctypes.POINTER(SolveInfo)]),
     "gb300_post_elements": (_I, [ctypes.POINTER(TermBatch), _P, _P]),
     "gb300_post_points": (_I, [ctypes.POINTER(TermBatch), _P, _I, _P, _P, _P, _P]),

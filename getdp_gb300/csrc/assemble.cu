@@ -402,6 +402,86 @@ k_tet4_curlcurl(int ne, const double *__restrict__ nodes,
 }
 
 // ---------------------------------------------------------------------------
+// 2D nonlinear a_z, the Newton-Raphson formulation of
+// templates/Lib_Magnetostatics_a_phi.pro:186-193, at the current solution x:
+//   [ nu[{d a}] {d a}, {d a} ] + [ dhdb[{d a}] Dof{d a}, {d a} ]
+//   + [ -dhdb[{d a}] {d a}, {d a} ] + [ -js, {a} ]
+// nu(b) = nu0 / (1 + k exp(-|b|^2 / b2)), dhdb = nu I + 2 dnu/d|b|^2 b b^T.
+// {d a} is constant on a P1 triangle: evaluated once, used at every Gauss
+// point (the 3-point sums of the reference, over the same constant).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_tri3_nl(int ne, const double *__restrict__ nodes, const int *__restrict__ elems,
+          const int *__restrict__ edofs, const double *__restrict__ nu0,
+          const double *__restrict__ js, const double *__restrict__ sol, double k,
+          double b2, CsrView A, double *__restrict__ b)
+{
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if(e >= ne) return;
+  int v0 = elems[3 * e], v1 = elems[3 * e + 1], v2 = elems[3 * e + 2];
+  double x0 = nodes[3 * v0], y0 = nodes[3 * v0 + 1];
+  double c11 = -x0 + nodes[3 * v1], c21 = -x0 + nodes[3 * v2];
+  double c12 = -y0 + nodes[3 * v1 + 1], c22 = -y0 + nodes[3 * v2 + 1];
+  double D = c11 * c22 - c12 * c21;
+  double aD = fabs(D);
+  int d[3] = {edofs[3 * e], edofs[3 * e + 1], edofs[3 * e + 2]};
+  const double gu[3] = {-1., 1., 0.}, gv[3] = {-1., 0., 1.};
+  double cx[3], cy[3], bx = 0., by = 0.;
+#pragma unroll
+  for(int i = 0; i < 3; i++) {
+    double s0 = gv[i], s1 = -gu[i];
+    cx[i] = (s0 * c11 + s1 * c21) / D;
+    cy[i] = (s0 * c12 + s1 * c22) / D;
+    double a = (sol && d[i] >= 0) ? sol[d[i]] : 0.;
+    bx += a * cx[i];
+    by += a * cy[i];
+  }
+  double s = bx * bx + by * by;
+  double ex = exp(-s / b2);
+  double den = 1. + k * ex;
+  double n0 = nu0[e];
+  double nu = n0 / den;
+  double d2 = n0 * (k / b2) * ex / (den * den);
+  double t11 = nu + 2. * d2 * (bx * bx), t12 = 2. * d2 * (bx * by);
+  double t22 = nu + 2. * d2 * (by * by);
+  double F = 3. * (c_pt3 * aD);  // the three Gauss weights of a constant
+  double hb0 = nu * bx, hb1 = nu * by;
+  double tb0 = -(t11 * bx + t12 * by), tb1 = -(t12 * bx + t22 * by);
+  double rhs[3];
+#pragma unroll
+  for(int i = 0; i < 3; i++) {
+    if(d[i] < 0) continue;
+#pragma unroll
+    for(int j = 0; j < 3; j++) {
+      if(d[j] < 0) continue;
+      double tc0 = t11 * cx[j] + t12 * cy[j], tc1 = t12 * cx[j] + t22 * cy[j];
+      scatter(A, d[i], d[j], F * (cx[i] * tc0 + cy[i] * tc1));
+    }
+  }
+  const double js_e = js ? js[e] : 0.;
+#pragma unroll
+  for(int i = 0; i < 3; i++) {
+    // -(E1 + E3) from the two explicit terms, + the source (N_i integrates
+    // to |D| / 6 on the three Gauss points: weights 1/6 at (1-u-v, u, v))
+    double e1 = F * (cx[i] * hb0 + cy[i] * hb1);
+    double e3 = F * (cx[i] * tb0 + cy[i] * tb1);
+    double es = 0.;
+    if(js_e != 0.) {
+#pragma unroll
+      for(int q = 0; q < 3; q++) {
+        double u = c_xt3[q], v = c_yt3[q];
+        double n[3] = {1. - u - v, u, v};
+        es += (c_pt3 * aD) * (n[i] * (-js_e));
+      }
+    }
+    rhs[i] = -e1 - e3 - es;
+  }
+#pragma unroll
+  for(int i = 0; i < 3; i++)
+    if(d[i] >= 0 && rhs[i] != 0.) atomicAdd(&b[d[i]], rhs[i]);
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 struct BatchDev {
@@ -422,6 +502,7 @@ static int term_shape(const gb300_term_batch *t, int *nv, int *nloc)
   case GB300_TERM_TRI3_EDDY_COMPLEX: *nv = 3; *nloc = 3; return GB300_OK;
   case GB300_TERM_TET10_ELASTICITY: *nv = 10; *nloc = 30; return GB300_OK;
   case GB300_TERM_TET4_EDGE_CURLCURL: *nv = 4; *nloc = 6; return GB300_OK;
+  case GB300_TERM_TRI3_MAGNETOSTATIC_NL: *nv = 3; *nloc = 3; return GB300_OK;
   default: set_error("unknown term kind %d", t->kind); return GB300_ERR_ARG;
   }
 }
@@ -504,8 +585,13 @@ int generate_pattern(gb300_matrix *A, const gb300_term_batch *t)
   return GB300_OK;
 }
 
-int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t)
+int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t,
+                    const gb300_vector *x)
 {
+  if(x && x->n != A->n) {
+    set_error("solution size %d != matrix size %d", x->n, A->n);
+    return GB300_ERR_ARG;
+  }
   if(!A->csr_valid) {
     set_error("matrix has no pattern: call gb300_generate_pattern first");
     return GB300_ERR_ARG;
@@ -539,6 +625,12 @@ int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t)
     case GB300_TERM_TET10_ELASTICITY:
       k_tet10_elasticity<<<grid_for(ne, kElWarps), 32 * kElWarps, 0, st>>>(
         ne, B.p_nodes, B.p_elems, B.p_edofs, B.p_coef, t->p0, t->p1, V, b->d.p);
+      break;
+    case GB300_TERM_TRI3_MAGNETOSTATIC_NL:
+      k_tri3_nl<<<grid_for(ne, 256), 256, 0, st>>>(ne, B.p_nodes, B.p_elems, B.p_edofs,
+                                                    B.p_coef, B.p_source,
+                                                    x ? x->d.p : nullptr, t->p0, t->p1,
+                                                    V, b->d.p);
       break;
     case GB300_TERM_TET4_EDGE_CURLCURL:
       if(!B.p_esign) {

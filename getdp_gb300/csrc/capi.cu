@@ -365,6 +365,28 @@ int gb300_vector_norm2(const gb300_vector *v, double *norm)
   return norm2_dev(v->n, v->d.p, norm, W, v->ctx->stream);
 }
 
+__global__ void k_axpby(int n, double a, const double *x, double b, double *y)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i < n) y[i] = (b == 0. ? 0. : b * y[i]) + a * x[i];
+}
+
+int gb300_vector_axpby(double a, const gb300_vector *x, double b, gb300_vector *y)
+{
+  GB_TRY(check(x, "x"));
+  GB_TRY(check(y, "y"));
+  if(x->n != y->n) {
+    set_error("vector sizes %d and %d differ", x->n, y->n);
+    return GB300_ERR_ARG;
+  }
+  if(y->n == 0) return GB300_OK;
+  cudaStream_t st = y->ctx->stream;
+  k_axpby<<<grid_for(y->n, 256), 256, 0, st>>>(y->n, a, x->d.p, b, y->d.p);
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(st));
+  return GB300_OK;
+}
+
 int gb300_vector_add_values(gb300_vector *v, int count, const int *idx,
                             const double *val)
 {
@@ -662,7 +684,17 @@ int gb300_generate_values(gb300_matrix *A, gb300_vector *b,
   GB_TRY(check(A, "matrix"));
   GB_TRY(check(b, "rhs"));
   GB_TRY(check(t, "term batch"));
-  return generate_values(A, b, t);
+  return generate_values(A, b, t, nullptr);
+}
+
+int gb300_generate_values_at(gb300_matrix *A, gb300_vector *b,
+                             const gb300_term_batch *t, const gb300_vector *x)
+{
+  GB_TRY(check(A, "matrix"));
+  GB_TRY(check(b, "rhs"));
+  GB_TRY(check(t, "term batch"));
+  GB_TRY(check(x, "solution"));
+  return generate_values(A, b, t, x);
 }
 
 // ----------------------------------------------------------- measurement

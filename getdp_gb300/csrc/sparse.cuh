@@ -34,7 +34,8 @@ void dot_part64(int n, const double *x, const double *y, double *part,
 void dot_part32(int n, const float *x, const float *y, double *part,
                 cudaStream_t st);
 
-int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t);
+int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t,
+                    const gb300_vector *x);
 int generate_pattern(gb300_matrix *A, const gb300_term_batch *t);
 
 struct ilu_data;

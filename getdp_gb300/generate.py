@@ -45,6 +45,11 @@ def term_arrays(p: Problem, dm: DofMap) -> dict:
         kind = _lib.TERM_TET10_ELASTICITY
         p0 = p.params["poisson"]
         p1 = -p.params["rho"] * p.params["g"]
+    elif f == "nonlinear2d":
+        kind = _lib.TERM_TRI3_MAGNETOSTATIC_NL
+        a["source"] = np.ascontiguousarray(p.source, np.float64)
+        p0 = p.params["k_sat"]
+        p1 = p.params["b_sat2"]
     elif f == "curlcurl":
         kind = _lib.TERM_TET4_EDGE_CURLCURL
         a["elem_sign"] = np.ascontiguousarray(dm.elem_sign, np.int8)
@@ -109,8 +114,10 @@ def host_batch(arrays: dict) -> TermBatch:
     return _batch(arrays, ptrs, 0)
 
 
-def generate(A: gMatrix, b: gVector, batch: TermBatch, pattern: bool = True) -> None:
-    """Generate[A]: (re)build A's pattern if asked, zero A and b, assemble."""
+def generate(A: gMatrix, b: gVector, batch: TermBatch, pattern: bool = True,
+             solution: gVector = None) -> None:
+    """Generate[A]: (re)build A's pattern if asked, zero A and b, assemble
+    (at the current solution, for a formulation that depends on it)."""
     L = _lib.load()
     if pattern:
         check(L.gb300_generate_pattern(A.h, ctypes.byref(batch)))
@@ -121,7 +128,11 @@ def generate(A: gMatrix, b: gVector, batch: TermBatch, pattern: bool = True) -> 
     if not pattern:
         # values only: zero the existing pattern's values
         check(L.gb300_matrix_zero(A.h))
-    check(L.gb300_generate_values(A.h, b.h, ctypes.byref(batch)))
+    if solution is None:
+        check(L.gb300_generate_values(A.h, b.h, ctypes.byref(batch)))
+    else:
+        solution._flush()
+        check(L.gb300_generate_values_at(A.h, b.h, ctypes.byref(batch), solution.h))
 
 
 def generate_problem(p: Problem, dm: DofMap, A: gMatrix = None, b: gVector = None):

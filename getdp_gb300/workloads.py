@@ -207,6 +207,53 @@ def magnetostatics_2d(n: int, seed: int = 1, jitter: float = 0.2) -> Problem:
                    {"n": n, "seed": seed, "jitter": jitter})
 
 
+def gaussian_field(points: np.ndarray, seed: int, corr: float,
+                   grid: int = 256) -> np.ndarray:
+    """Unit-variance Gaussian random field with covariance exp(-d^2 / (2
+    corr^2)) on the unit square, sampled at points (nearest node of a
+    periodic FFT grid of grid^2 nodes)."""
+    rng = np.random.default_rng(seed)
+    k = np.fft.fftfreq(grid, d=1.0 / grid) * 2.0 * np.pi
+    kx, ky = np.meshgrid(k, k, indexing="ij")
+    spec = np.exp(-0.25 * corr * corr * (kx * kx + ky * ky))  # sqrt of the PSD
+    noise = rng.standard_normal((grid, grid))
+    f = np.real(np.fft.ifft2(np.fft.fft2(noise) * spec))
+    f = (f - f.mean()) / f.std()
+    i = np.clip(np.rint(points[:, 0] * (grid - 1)).astype(int), 0, grid - 1)
+    j = np.clip(np.rint(points[:, 1] * (grid - 1)).astype(int), 0, grid - 1)
+    return f[i, j]
+
+
+def nonlinear_2d(n: int, seed: int = 5, jitter: float = 0.2, corr: float = 0.05,
+                 sigma_log: float = 1.0, n_blobs: int = 8,
+                 blob_radius: float = 0.02) -> Problem:
+    """Nonlinear a_z P1 magnetostatics on the unit square.
+
+    nu(x, |B|) = nu0(x) (1 + 999 exp(-|B|^2 / 1.5^2))^-1 with nu0 =
+    exp(sigma_log g(x)) / mu0, g a seeded Gaussian random field of
+    correlation length corr (per element, at the centroid); J_z = sum of
+    n_blobs seeded Gaussian blobs of amplitude +-1e6 A/m^2 and radius
+    blob_radius (per element at the centroid); a = 0 on the boundary.
+    Newton on the reference's Newton-Raphson formulation
+    (Lib_Magnetostatics_a_phi.pro: nu[{d a}] {d a} + dhdb[{d a}] (Dof{d a}
+    - {d a})).
+    """
+    m = square_tri_mesh(n, seed, jitter)
+    c = m.nodes[m.elems].mean(axis=1)
+    nu0 = np.exp(sigma_log * gaussian_field(c, seed + 1, corr)) / MU0
+    rng = np.random.default_rng(seed + 2)
+    js = np.zeros(m.n_elems)
+    for _ in range(n_blobs):
+        cx, cy = rng.uniform(0.15, 0.85, 2)
+        s = rng.choice([-1.0, 1.0])
+        js += s * 1.0e6 * np.exp(-((c[:, 0] - cx) ** 2 + (c[:, 1] - cy) ** 2) /
+                                 (2 * blob_radius ** 2))
+    m.region = np.full(m.n_elems, 1, np.int32)
+    return Problem(f"nonlinear2d_n{n}", m, "nonlinear2d", nu0, js,
+                   {"n": n, "seed": seed, "jitter": jitter, "b_sat2": 1.5 ** 2,
+                    "k_sat": 999.0})
+
+
 def elasticity_p2(n: int, seed: int = 2, sigma_log: float = 0.5) -> Problem:
     """3D linear elasticity, 10-node tetrahedra, per-element lognormal E.
 
@@ -388,6 +435,8 @@ def dofmap_for(p: Problem) -> DofMap:
         return nodal_dofmap(p.mesh)
     if p.formulation == "eddy2d":
         return nodal_dofmap(p.mesh, nharm=2)
+    if p.formulation == "nonlinear2d":
+        return nodal_dofmap(p.mesh)
     if p.formulation == "elasticity":
         return nodal_dofmap(p.mesh, ncomp=3)
     if p.formulation == "curlcurl":
@@ -545,6 +594,59 @@ Formulation {{ {{ Name F; Type FemEquation;
 Resolution {{ {{ Name R; System {{ {system} }}
   Operation {{ {_DUMP_OPS} }} }} }}
 """
+    if f == "nonlinear2d":
+        ne = p.mesh.n_elems
+        lines = []
+        for k in range(ne):
+            lines.append(f"  nu0[Region[{1000 + k}]] = {p.coef[k]:.17g};")
+            lines.append(f"  js[Region[{1000 + k}]] = Vector[0, 0, {p.source[k]:.17g}];")
+        b2, ks = p.params["b_sat2"], p.params["k_sat"]
+        tol = p.params.get("nl_tol", 1e-8)
+        itmax = p.params.get("nl_iter_max", 50)
+        res_fmt = 'Format "Residual %03g: abs %14.12e rel %14.12e"'
+        return f"""Group {{
+  Vol = Region[{{{1000}:{1000 + ne - 1}}}]; Bnd = Region[10];
+}}
+Function {{
+{chr(10).join(lines)}
+  nu[] = nu0[] / (1. + {ks:.17g} * Exp[-SquNorm[$1] / {b2:.17g}]);
+  dnudb2[] = nu0[] * ({ks:.17g} / {b2:.17g}) * Exp[-SquNorm[$1] / {b2:.17g}] /
+             (1. + {ks:.17g} * Exp[-SquNorm[$1] / {b2:.17g}])^2;
+  dhdb[] = TensorDiag[1, 1, 1] * nu[$1] + 2. * dnudb2[$1] * SquDyadicProduct[$1];
+}}
+Constraint {{ {{ Name a; Case {{ {{ Region Bnd; Value 0.; }} }} }} }}
+FunctionSpace {{
+  {{ Name Hcurl_a; Type Form1P;
+    BasisFunction {{ {{ Name se; NameOfCoef ae; Function BF_PerpendicularEdge;
+      Support Vol; Entity NodesOf[All]; }} }}
+    Constraint {{ {{ NameOfCoef ae; EntityType NodesOf; NameOfConstraint a; }} }} }}
+}}
+Jacobian {{ {{ Name Vol; Case {{ {{ Region All; Jacobian Vol; }} }} }} }}
+Integration {{ {{ Name I1; Case {{ {{ Type Gauss;
+  Case {{ {{ GeoElement Triangle; NumberOfPoints 3; }} }} }} }} }} }}
+Formulation {{ {{ Name F; Type FemEquation;
+  Quantity {{ {{ Name a; Type Local; NameOfSpace Hcurl_a; }} }}
+  Equation {{
+    Integral {{ [ nu[{{d a}}] * {{d a}}, {{d a}} ]; In Vol; Jacobian Vol; Integration I1; }}
+    Integral {{ [ dhdb[{{d a}}] * Dof{{d a}}, {{d a}} ]; In Vol; Jacobian Vol; Integration I1; }}
+    Integral {{ [ -dhdb[{{d a}}] * {{d a}}, {{d a}} ]; In Vol; Jacobian Vol; Integration I1; }}
+    Integral {{ [ -js[], {{a}} ]; In Vol; Jacobian Vol; Integration I1; }}
+  }} }} }}
+Resolution {{ {{ Name R; System {{ {{ Name A; NameOfFormulation F; }} }}
+  Operation {{
+    InitSolution[A];
+    Generate[A]; Write[A, File "b.bin"]; Solve[A];
+    Generate[A]; GetResidual[A, $res0];
+    Evaluate[ $res = $res0, $iter = 0 ];
+    Print[{{$iter, $res, $res / $res0}}, {res_fmt}];
+    While[$res > 1e-300 && $res / $res0 > {tol:.17g} && $res / $res0 <= 1 && $iter < {itmax}]{{
+      Solve[A]; Generate[A]; GetResidual[A, $res];
+      Evaluate[ $iter = $iter + 1 ];
+      Print[{{$iter, $res, $res / $res0}}, {res_fmt}];
+    }}
+    SaveSolution[A];
+  }} }} }}
+"""
     if f == "elasticity":
         ne = p.mesh.n_elems
         pois = p.params["poisson"]
@@ -666,7 +768,7 @@ PostOperation {{ {{ Name Map; NameOfPostProcessing P;
 
 def write_pro(p: Problem, path: str) -> None:
     """Write the problem file; elasticity needs one region per element."""
-    if p.formulation == "elasticity":
+    if p.formulation in ("elasticity", "nonlinear2d"):
         p.mesh.region = (1000 + np.arange(p.mesh.n_elems)).astype(np.int32)
     with open(path, "w") as f:
         f.write(pro_text(p))

@@ -124,6 +124,10 @@ int gb300_vector_get(const gb300_vector *v, double *host);
 int gb300_vector_size(const gb300_vector *v, int *n);
 /* LinAlg_VectorNorm2 (norm2_vector) */
 int gb300_vector_norm2(const gb300_vector *v, double *norm);
+/* y = a x + b y on the device (x and y of the same size, x may be y):
+   LinAlg_CopyVector (a = 1, b = 0), LinAlg_ProdVectorDouble (x = y, b = 0)
+   and LinAlg_AddVectorProdVectorDouble (b = 1), LinAlg.h:159-175 */
+int gb300_vector_axpby(double a, const gb300_vector *x, double b, gb300_vector *y);
 /* LinAlg_AddScalarInVector / AddDoubleInVector for a batch of entries
    (host arrays), added in order */
 int gb300_vector_add_values(gb300_vector *v, int count, const int *idx,
@@ -183,6 +187,13 @@ int gb300_matrix_mult(gb300_matrix *A, const gb300_vector *x, gb300_vector *y);
 /*   3D Whitney edges (BF_Edge) on 4-node tets, 4-point Gauss:
      [coef * Dof{d a}, {d a}] + [p0 * coef * Dof{a}, {a}] + [-js, {a}],
      js = p1 * (-(y-0.5), x-0.5, 0) / r in elements with source != 0 */
+#define GB300_TERM_TRI3_MAGNETOSTATIC_NL 5
+/*   2D a_z as TRI3_MAGNETOSTATIC with a field-dependent reluctivity, the
+     Newton-Raphson terms of templates/Lib_Magnetostatics_a_phi.pro:186-193
+     at the current solution (gb300_generate_values_at):
+     [nu(b) b, {d a}] + [dhdb(b) Dof{d a}, {d a}] + [-dhdb(b) b, {d a}]
+     + [-source, {a}], b = {d a}, nu(b) = coef / (1 + p0 exp(-|b|^2 / p1)),
+     dhdb = nu I + 2 dnu/d|b|^2 b b^T */
 
 typedef struct gb300_term_batch {
   int kind;
@@ -210,6 +221,11 @@ int gb300_generate_pattern(gb300_matrix *A, const gb300_term_batch *t);
    contain the element pairs: gb300_generate_pattern). */
 int gb300_generate_values(gb300_matrix *A, gb300_vector *b,
                           const gb300_term_batch *t);
+/* The same at the current solution x (Generate of a nonlinear problem
+   evaluates its coefficients from Current.DofData->CurrentSolution);
+   formulations that do not depend on x ignore it. */
+int gb300_generate_values_at(gb300_matrix *A, gb300_vector *b,
+                             const gb300_term_batch *t, const gb300_vector *x);
 
 /* ---- post-processing ------------------------------------------------- */
 /* PostOperation Print[ {d a}, OnElementsOf ... ] (Pos_Print.cpp,

@@ -63,6 +63,7 @@ def lib(ilu: str = "64") -> ctypes.CDLL:
         L.oracle_assemble_tri_p1.restype = i64
         L.oracle_assemble_tet10_elasticity.restype = i64
         L.oracle_assemble_tet4_curlcurl.restype = i64
+        L.oracle_assemble_tri3_nl.restype = i64
         L.oracle_coo_to_csr.restype = i64
         L.oracle_solve_csr.restype = ctypes.c_int
         _LIBS[ilu] = L
@@ -73,9 +74,10 @@ def _p(a, ct):
     return a.ctypes.data_as(ctypes.POINTER(ct))
 
 
-def assemble(problem, dofmap, ilu: str = "64"):
-    """Run the restated element loop; returns (indptr, indices, data, b)."""
-    rr, cc, vv, b = assemble_coo(problem, dofmap, ilu)
+def assemble(problem, dofmap, ilu: str = "64", solution=None):
+    """Run the restated element loop (at the current solution, for the
+    nonlinear formulation); returns (indptr, indices, data, b)."""
+    rr, cc, vv, b = assemble_coo(problem, dofmap, ilu, solution)
     L = lib(ilu)
     I32, D = ctypes.c_int32, ctypes.c_double
     n = dofmap.n_dof
@@ -89,7 +91,7 @@ def assemble(problem, dofmap, ilu: str = "64"):
     return indptr, indices[:nnz].copy(), data[:nnz].copy(), b
 
 
-def assemble_coo(problem, dofmap, ilu: str = "64"):
+def assemble_coo(problem, dofmap, ilu: str = "64", solution=None):
     """The matrix contributions in the reference's call order (the
     LinAlg_AddDoubleInMatrix sequence) and the RHS: (rows, cols, vals, b)."""
     L = lib(ilu)
@@ -135,6 +137,14 @@ def assemble_coo(problem, dofmap, ilu: str = "64"):
             _p(np.ascontiguousarray(problem.source, np.float64), D),
             ctypes.c_double(problem.params["reg"]), ctypes.c_double(problem.params["J0"]),
             ctypes.c_int64(cap), _p(rr, I32), _p(cc, I32), _p(vv, D), _p(b, D))
+    elif f == "nonlinear2d":
+        x = np.zeros(n) if solution is None else np.ascontiguousarray(solution, np.float64)
+        nz = L.oracle_assemble_tri3_nl(
+            ne, _p(nodes, D), _p(elems, ctypes.c_int), _p(edofs, ctypes.c_int),
+            _p(np.ascontiguousarray(problem.coef, np.float64), D),
+            _p(np.ascontiguousarray(problem.source, np.float64), D), _p(x, D),
+            ctypes.c_double(problem.params["k_sat"]), ctypes.c_double(problem.params["b_sat2"]),
+            ctypes.c_int64(cap), _p(rr, I32), _p(cc, I32), _p(vv, D), _p(b, D))
     else:
         raise ValueError(f)
     if nz > cap:
@@ -179,3 +189,66 @@ def params_from_golden(keys, vals) -> dict:
     out.setdefault("scaling", 0)
     out.setdefault("renumbering", 1)
     return out
+
+
+def newton(problem, dofmap, tol=1e-8, iter_max=50, relaxation=(1.0,), **solve_kw):
+    """The Newton loop of the reference's nonlinear resolution
+    (Lib_Magnetostatics_a_phi.pro:220-240): Generate; Solve; Generate;
+    GetResidual; While[res > 0 && res/res0 > tol && res/res0 <= 1 &&
+    iter < iter_max] { Solve; Generate; GetResidual }.  GetResidual is
+    ||b - A x||_2 (SolvingOperations.cpp:1318-1341).  With several
+    relaxation factors, each Solve's step dx = x_new - x is relaxed as
+    SolveJac_AdaptRelax does with CheckAll 0 (SolvingOperations.cpp:
+    1593-1700): factors tried in order, the residual ||b - A x|| / N at
+    x + f dx (regenerated there) kept while it decreases, the best factor
+    taken.  Returns (x, residual history, linear iterations per solve)."""
+    import scipy.sparse as sp
+    n = dofmap.n_dof
+    x = np.zeros(n)
+    its = []
+
+    def gen(xc):
+        ip, ix, dv, bb = assemble(problem, dofmap, solution=xc)
+        return ip, ix, dv, bb
+
+    def sol(sysm):
+        ip, ix, dv, bb = sysm
+        xs, st, k, _ = solve(ip, ix, dv, bb, **solve_kw)
+        if st != 0:
+            raise RuntimeError(f"oracle linear solve failed ({st})")
+        its.append(k)
+        return xs
+
+    def resid(sysm, xc):
+        ip, ix, dv, bb = sysm
+        A = sp.csr_matrix((dv, ix, ip), shape=(n, n))
+        return float(np.linalg.norm(bb - A @ xc))
+
+    def step(sysm, x):
+        xn = sol(sysm)
+        if len(relaxation) == 1:
+            return xn, gen(xn)
+        dx = xn - x
+        err_prev, f_opt, best = 1e99, relaxation[0], None
+        for k, f in enumerate(relaxation):
+            xt = x + f * dx
+            st = gen(xt)
+            e = resid(st, xt) / n
+            if e < err_prev:
+                err_prev, f_opt, best = e, f, (xt, st)
+            elif k > 0:
+                break
+        return best
+
+    sysm = gen(x)
+    x, sysm = step(sysm, x)
+    res0 = resid(sysm, x)
+    hist = [res0]
+    res, it = res0, 0
+    while res > 1e-300 and res / res0 > tol and res / res0 <= 1 and it < iter_max:
+        x, sysm = step(sysm, x)
+        res = resid(sysm, x)
+        it += 1
+        hist.append(res)
+    return x, np.array(hist), its
+

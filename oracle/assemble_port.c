@@ -220,6 +220,93 @@ static void tri_curl(const M3 *J, double D, int i, double out[3])
   out[2] = 0.;
 }
 
+/* Nonlinear a_z (the Newton-Raphson formulation of
+   templates/Lib_Magnetostatics_a_phi.pro:186-193) at the current solution x:
+     [ nu[{d a}] * {d a}, {d a} ]       NoDof: b -= E
+     [ dhdb[{d a}] * Dof{d a}, {d a} ]  matrix (full, row-major call order)
+     [ -dhdb[{d a}] * {d a}, {d a} ]    NoDof: b -= E
+     [ -js[], {a} ]                     NoDof
+   with the .pro functions nu[] = nu0 / (1 + k exp(-|b|^2 / b2)),
+   dnudb2[] = nu0 (k / b2) exp(-|b|^2 / b2) / (1 + k exp(...))^2,
+   dhdb[] = TensorDiag[1,1,1] nu[b] + 2 dnudb2[b] SquDyadicProduct[b];
+   {d a} at a Gauss point = sum_i x_i curl(N_i e_z) (fixed DOFs 0). */
+static void nl_law(double nu0, double k, double b2, const double bv[3],
+                   double *nu, double T[3][3])
+{
+  double s = bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2];
+  double ex = exp(-s / b2);
+  double den = 1. + k * ex;
+  *nu = nu0 / den;
+  double d2 = nu0 * (k / b2) * ex / (den * den);
+  int a, c;
+  for(a = 0; a < 3; a++)
+    for(c = 0; c < 3; c++) T[a][c] = (a == c ? *nu : 0.) + 2. * d2 * (bv[a] * bv[c]);
+}
+
+int64_t oracle_assemble_tri3_nl(int ne, const double *nodes, const int *elems,
+                                const int *edofs, const double *nu0,
+                                const double *js, const double *sol, double k,
+                                double b2, int64_t cap, int32_t *rr, int32_t *cc,
+                                double *vv, double *b)
+{
+  Coo m = {0, cap, rr, cc, vv};
+  int e, q, i, j, c;
+  for(e = 0; e < ne; e++) {
+    const int *el = elems + 3 * e;
+    const int *dof = edofs + 3 * e;
+    double Ek[3][3], Eb1[3] = {0., 0., 0.}, Eb3[3] = {0., 0., 0.};
+    double x[3], y[3], n[3], D, F;
+    M3 J;
+    for(i = 0; i < 3; i++)
+      for(j = 0; j < 3; j++) Ek[i][j] = 0.;
+    for(q = 0; q < 3; q++) {
+      double cE[3][3], bv[3] = {0., 0., 0.}, T[3][3], nu, hb[3], tb[3];
+      tri_geom(nodes, el, q, x, y, &J, &D, n);
+      for(i = 0; i < 3; i++) tri_curl(&J, D, i, cE[i]);
+      for(i = 0; i < 3; i++) {
+        double a = dof[i] >= 0 ? sol[dof[i]] : 0.;
+        for(c = 0; c < 3; c++) bv[c] += a * cE[i][c];
+      }
+      nl_law(nu0[e], k, b2, bv, &nu, T);
+      F = 1. * (PT3[q] * fabs(D));
+      for(c = 0; c < 3; c++) {
+        hb[c] = nu * bv[c];
+        tb[c] = -(T[c][0] * bv[0] + T[c][1] * bv[1] + T[c][2] * bv[2]);
+      }
+      for(i = 0; i < 3; i++) {
+        Eb1[i] += F * dot3(cE[i], hb);
+        Eb3[i] += F * dot3(cE[i], tb);
+        for(j = 0; j < 3; j++) {
+          double tc[3];
+          for(c = 0; c < 3; c++)
+            tc[c] = T[c][0] * cE[j][0] + T[c][1] * cE[j][1] + T[c][2] * cE[j][2];
+          Ek[i][j] += F * dot3(cE[i], tc);
+        }
+      }
+    }
+    for(i = 0; i < 3; i++)
+      if(dof[i] >= 0 && Eb1[i]) b[dof[i]] += (1. * 1.) * -Eb1[i];
+    for(i = 0; i < 3; i++)
+      for(j = 0; j < 3; j++)
+        if(dof[i] >= 0 && dof[j] >= 0) coo_add(&m, dof[i], dof[j], Ek[i][j]);
+    for(i = 0; i < 3; i++)
+      if(dof[i] >= 0 && Eb3[i]) b[dof[i]] += (1. * 1.) * -Eb3[i];
+    if(js[e] != 0.) {
+      double Es[3] = {0., 0., 0.};
+      for(q = 0; q < 3; q++) {
+        tri_geom(nodes, el, q, x, y, &J, &D, n);
+        F = 1. * (PT3[q] * fabs(D));
+        for(i = 0; i < 3; i++) Es[i] += F * ((n[i] / J.c33) * (-js[e]));
+      }
+      for(i = 0; i < 3; i++) {
+        if(dof[i] < 0 || !Es[i]) continue;
+        b[dof[i]] += (1. * 1.) * -Es[i];
+      }
+    }
+  }
+  return m.n;
+}
+
 int64_t oracle_assemble_tri_p1(int ne, const double *nodes, const int *elems,
                                const int *edofs, const double *nu,
                                const double *js, const double *sigma,

@@ -12,10 +12,11 @@ _GEN = {"ms2d": W.magnetostatics_2d, "el": W.elasticity_p2,
 
 
 def names():
-    """The solve fixtures (post-processing fixtures are post_*.npz)."""
+    """The solve fixtures (post-processing and Newton fixtures are
+    post_*.npz and newton_*.npz)."""
     return sorted(os.path.basename(f)[:-4]
                   for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(f).startswith("post_"))
+                  if not os.path.basename(f).startswith(("post_", "newton_")))
 
 
 def load(name):
