@@ -175,104 +175,164 @@ __device__ __forceinline__ double wsum_all(double v)
   return v;
 }
 
+// node pairs (a, b), a <= b, of the 10-node tetrahedron
+__constant__ signed char c_pair_a[55] = {
+  0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 2, 2, 2, 3,
+  3, 3, 3, 3, 3, 3, 4, 4, 4, 4, 4, 4, 5, 5, 5, 5, 5, 6, 6, 6, 6, 7, 7, 7, 8, 8, 9};
+__constant__ signed char c_pair_b[55] = {
+  0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 1, 2, 3, 4, 5, 6, 7, 8, 9, 2, 3, 4, 5, 6, 7, 8, 9, 3,
+  4, 5, 6, 7, 8, 9, 4, 5, 6, 7, 8, 9, 5, 6, 7, 8, 9, 6, 7, 8, 9, 7, 8, 9, 8, 9, 9};
+
+// The nine terms [-C_ij Dof{d u_j}, {d u_i}] of Lib_Elasticity_u.pro with the
+// isotropic tensors (a = E(1-nu)/(1+nu)/(1-2nu), c = E nu/(1+nu)/(1-2nu),
+// b = E/2/(1+nu)) give, for the node pair (a, b) and Gauss-weighted
+// gradients, the 3 x 3 block
+//   K_ij = -(b tr(M) delta_ij + c M_ij + b M_ji),  M_ij = sum_q F_q g_a,i g_b,j
+// (the diagonal term a g_a,i g_b,i + b sum_{k != i} g_a,k g_b,k equals
+// b (g_a . g_b) + (c + b) g_a,i g_b,i, as a = c + 2b).  K_ba = K_ab^T, so
+// only the 55 pairs a <= b are evaluated.  One warp per element: the four
+// Gauss points' Jacobians on lanes 0-3, the 40 (point, node) gradients on
+// all lanes, then the pairs.
+//
+// B3: the pattern holds 3 x 3 node blocks (checked from the element table:
+// component c of node a is row a + c nn for every node with unknowns), so
+// the nine entries of a node pair sit at rowptr[row(a, c)] + c' L_a +
+// pos_a(b): one search per node pair instead of nine.
+template <int B3>
 __global__ void __launch_bounds__(32 * kElWarps)
 k_tet10_elasticity(int ne, const double *__restrict__ nodes,
                    const int *__restrict__ elems, const int *__restrict__ edofs,
                    const double *__restrict__ E, double poisson, double fz,
                    CsrView A, double *__restrict__ b)
 {
-  __shared__ double sg[kElWarps][4][10][3];
+  __shared__ double sx[kElWarps][10][3];
+  __shared__ double sinv[kElWarps][4][9];
   __shared__ double sF[kElWarps][4];
+  __shared__ double sg[kElWarps][4][10][3];   // gradients
+  __shared__ double sgF[kElWarps][4][10][3];  // gradients x F_q
   __shared__ int sd[kElWarps][30];
   int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int e = blockIdx.x * kElWarps + w;
   if(e >= ne) return;  // warp-uniform
-  double x = 0., y = 0., z = 0.;
   if(lane < 10) {
     int v = elems[10 * e + lane];
-    x = nodes[3 * v];
-    y = nodes[3 * v + 1];
-    z = nodes[3 * v + 2];
+    sx[w][lane][0] = nodes[3 * v];
+    sx[w][lane][1] = nodes[3 * v + 1];
+    sx[w][lane][2] = nodes[3 * v + 2];
   }
   if(lane < 30) sd[w][lane] = edofs[30 * e + lane];
-  double eb = 0.;  // body-force integral of node `lane`
-  for(int q = 0; q < 4; q++) {
-    double s[3], N;
-    tet10_dndu(lane < 10 ? lane : 10, c_xtet4[q], c_ytet4[q], c_ztet4[q], s, &N);
-    double c11 = wsum_all(x * s[0]), c21 = wsum_all(x * s[1]), c31 = wsum_all(x * s[2]);
-    double c12 = wsum_all(y * s[0]), c22 = wsum_all(y * s[1]), c32 = wsum_all(y * s[2]);
-    double c13 = wsum_all(z * s[0]), c23 = wsum_all(z * s[1]), c33 = wsum_all(z * s[2]);
-    double D = c11 * c22 * c33 + c13 * c21 * c32 + c12 * c23 * c31 -
-               c13 * c22 * c31 - c11 * c23 * c32 - c12 * c21 * c33;
-    double i11 = (c22 * c33 - c23 * c32) / D;
-    double i21 = -(c21 * c33 - c23 * c31) / D;
-    double i31 = (c21 * c32 - c22 * c31) / D;
-    double i12 = -(c12 * c33 - c13 * c32) / D;
-    double i22 = (c11 * c33 - c13 * c31) / D;
-    double i32 = -(c11 * c32 - c12 * c31) / D;
-    double i13 = (c12 * c23 - c13 * c22) / D;
-    double i23 = -(c11 * c23 - c13 * c21) / D;
-    double i33 = (c11 * c22 - c12 * c21) / D;
-    double F = c_ptet4 * fabs(D);
-    if(lane < 10) {
-      sg[w][q][lane][0] = s[0] * i11 + s[1] * i12 + s[2] * i13;
-      sg[w][q][lane][1] = s[0] * i21 + s[1] * i22 + s[2] * i23;
-      sg[w][q][lane][2] = s[0] * i31 + s[1] * i32 + s[2] * i33;
-      eb += F * (N * fz);
+  __syncwarp();
+  if(lane < 4) {
+    // JacobianVol3D at Gauss point q: c_rc = sum_k x_k,c dN_k/du_r
+    const int q = lane;
+    double c[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}};
+    for(int k = 0; k < 10; k++) {
+      double s[3], N;
+      tet10_dndu(k, c_xtet4[q], c_ytet4[q], c_ztet4[q], s, &N);
+#pragma unroll
+      for(int r = 0; r < 3; r++)
+#pragma unroll
+        for(int cc = 0; cc < 3; cc++) c[r][cc] += sx[w][k][cc] * s[r];
     }
-    if(lane == 0) sF[w][q] = F;
+    double D = c[0][0] * c[1][1] * c[2][2] + c[0][2] * c[1][0] * c[2][1] +
+               c[0][1] * c[1][2] * c[2][0] - c[0][2] * c[1][1] * c[2][0] -
+               c[0][0] * c[1][2] * c[2][1] - c[0][1] * c[1][0] * c[2][2];
+    double iD = 1. / D;
+    double *I = sinv[w][q];
+    // i_ab (a physical, b reference): the inverse of the Jacobian
+    I[0] = (c[1][1] * c[2][2] - c[1][2] * c[2][1]) * iD;     // i11
+    I[1] = -(c[0][1] * c[2][2] - c[0][2] * c[2][1]) * iD;    // i12
+    I[2] = (c[0][1] * c[1][2] - c[0][2] * c[1][1]) * iD;     // i13
+    I[3] = -(c[1][0] * c[2][2] - c[1][2] * c[2][0]) * iD;    // i21
+    I[4] = (c[0][0] * c[2][2] - c[0][2] * c[2][0]) * iD;     // i22
+    I[5] = -(c[0][0] * c[1][2] - c[0][2] * c[1][0]) * iD;    // i23
+    I[6] = (c[1][0] * c[2][1] - c[1][1] * c[2][0]) * iD;     // i31
+    I[7] = -(c[0][0] * c[2][1] - c[0][1] * c[2][0]) * iD;    // i32
+    I[8] = (c[0][0] * c[1][1] - c[0][1] * c[1][0]) * iD;     // i33
+    sF[w][q] = c_ptet4 * fabs(D);
   }
   __syncwarp();
-  // Lib_Elasticity_u.pro: a = E(1-nu)/(1+nu)/(1-2nu), c = E nu/(1+nu)/(1-2nu),
-  // b = E/2/(1+nu)
+  for(int t = lane; t < 40; t += 32) {
+    int q = t / 10, a = t % 10;
+    double s[3], N;
+    tet10_dndu(a, c_xtet4[q], c_ytet4[q], c_ztet4[q], s, &N);
+    const double *I = sinv[w][q];
+    double F = sF[w][q];
+#pragma unroll
+    for(int r = 0; r < 3; r++) {
+      double g = s[0] * I[3 * r] + s[1] * I[3 * r + 1] + s[2] * I[3 * r + 2];
+      sg[w][q][a][r] = g;
+      sgF[w][q][a][r] = F * g;
+    }
+  }
+  __syncwarp();
   double Ee = E[e];
-  double ca = Ee * (1. - poisson) / (1. + poisson) / (1. - 2. * poisson);
   double cc = Ee * poisson / (1. + poisson) / (1. - 2. * poisson);
   double cb = Ee / 2. / (1. + poisson);
   const int *d = sd[w];
-  for(int p = lane; p < 100; p += 32) {
-    int a = p / 10, bn = p % 10;
+  for(int p = lane; p < 55; p += 32) {
+    const int a = c_pair_a[p], bn = c_pair_b[p];
+    double M[3][3];
+#pragma unroll
+    for(int i = 0; i < 3; i++)
+#pragma unroll
+      for(int j = 0; j < 3; j++) {
+        double m = 0.;
+#pragma unroll
+        for(int q = 0; q < 4; q++) m += sgF[w][q][a][i] * sg[w][q][bn][j];
+        M[i][j] = m;
+      }
+    const double tr = M[0][0] + M[1][1] + M[2][2];
     double K[3][3];
 #pragma unroll
     for(int i = 0; i < 3; i++)
 #pragma unroll
-      for(int j = 0; j < 3; j++) K[i][j] = 0.;
-#pragma unroll
-    for(int q = 0; q < 4; q++) {
-      double ga0 = sg[w][q][a][0], ga1 = sg[w][q][a][1], ga2 = sg[w][q][a][2];
-      double gb0 = sg[w][q][bn][0], gb1 = sg[w][q][bn][1], gb2 = sg[w][q][bn][2];
-      double F = sF[w][q];
-      double ga[3] = {ga0, ga1, ga2}, gbv[3] = {gb0, gb1, gb2};
-#pragma unroll
-      for(int i = 0; i < 3; i++)
-#pragma unroll
-        for(int j = 0; j < 3; j++) {
-          double t;
-          if(i == j) {
-            // g_a . diag(b,b,b with a at (i,i)) g_b
-            t = 0.;
-#pragma unroll
-            for(int k = 0; k < 3; k++) t += ga[k] * ((k == i ? ca : cb) * gbv[k]);
-          }
-          else {
-            // C_ij: c at (i,j), b at (j,i)
-            t = ga[i] * (cc * gbv[j]) + ga[j] * (cb * gbv[i]);
-          }
-          K[i][j] += F * (-t);
+      for(int j = 0; j < 3; j++)
+        K[i][j] = -((i == j ? cb * tr : 0.) + cc * M[i][j] + cb * M[j][i]);
+    // block (a, bn) = K, block (bn, a) = K^T
+    for(int side = 0; side < (a == bn ? 1 : 2); side++) {
+      const int ra = side ? bn : a, cb_ = side ? a : bn;
+      if(B3) {
+        int r0 = d[ra], c0 = d[cb_];
+        if(r0 < 0 || c0 < 0) continue;  // a node's components: all unknown or all fixed
+        int s0 = A.rowptr[r0];
+        int L = (A.rowptr[r0 + 1] - s0) / 3;
+        int pos = find_col(A.col, s0, s0 + L, c0);
+        if(pos < 0) {
+          atomicExch(A.err, 1);
+          continue;
         }
-    }
+        pos -= s0;
 #pragma unroll
-    for(int i = 0; i < 3; i++) {
-      int r = d[10 * i + a];
-      if(r < 0) continue;
+        for(int i = 0; i < 3; i++) {
+          int rs = A.rowptr[d[10 * i + ra]];
 #pragma unroll
-      for(int j = 0; j < 3; j++) {
-        int c = d[10 * j + bn];
-        if(c >= 0) scatter(A, r, c, K[i][j]);
+          for(int j = 0; j < 3; j++)
+            atomicAdd(&A.val[rs + j * L + pos], side ? K[j][i] : K[i][j]);
+        }
+      }
+      else {
+#pragma unroll
+        for(int i = 0; i < 3; i++) {
+          int r = d[10 * i + ra];
+          if(r < 0) continue;
+#pragma unroll
+          for(int j = 0; j < 3; j++) {
+            int c = d[10 * j + cb_];
+            if(c >= 0) scatter(A, r, c, side ? K[j][i] : K[i][j]);
+          }
+        }
       }
     }
   }
+  // body force [f, {u_z}]: b -= -sum_q F_q N_a(q) fz on the z rows
   if(lane < 10) {
+    double eb = 0.;
+    for(int q = 0; q < 4; q++) {
+      double s[3], N;
+      tet10_dndu(lane, c_xtet4[q], c_ytet4[q], c_ztet4[q], s, &N);
+      eb += sF[w][q] * (N * fz);
+    }
     int r = d[20 + lane];
     if(r >= 0 && eb != 0.) atomicAdd(&b[r], -eb);
   }
@@ -552,6 +612,41 @@ __global__ void k_flag_nonzero(int ne, const double *__restrict__ c,
   if(e < ne) f[e] = (c && c[e] != 0.) ? 1 : 0;
 }
 
+// Every element holds the three components of each of its nodes either all
+// as unknowns numbered a, a + nn, a + 2 nn (GetDP's component-major order,
+// nn = n / 3) or all fixed.  Then the rows of a node's three components
+// touch the same elements, and their sorted column lists are the node's
+// neighbours once per component, in the same order (3 x 3 node blocks).
+__global__ void k_check_elem_components(int ne, const int *__restrict__ edofs,
+                                        int nn, int *__restrict__ bad)
+{
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if(e >= ne) return;
+  for(int a = 0; a < 10; a++) {
+    int d0 = edofs[30 * e + a], d1 = edofs[30 * e + 10 + a], d2 = edofs[30 * e + 20 + a];
+    bool ok = (d0 < 0 && d1 < 0 && d2 < 0) ||
+              (d0 >= 0 && d0 < nn && d1 == d0 + nn && d2 == d0 + 2 * nn);
+    if(!ok) atomicExch(bad, 1);
+  }
+}
+
+static int node_components_ok(const gb300_matrix *A, int ne, const int *edofs, bool *ok)
+{
+  *ok = false;
+  if(A->n % 3 || A->n == 0) return GB300_OK;
+  cudaStream_t st = A->ctx->stream;
+  DevBuf<int> bad;
+  GB_TRY(bad.alloc(1));
+  GB_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
+  if(ne > 0)
+    k_check_elem_components<<<grid_for(ne, 256), 256, 0, st>>>(ne, edofs, A->n / 3, bad.p);
+  int hb = 0;
+  GB_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  *ok = (hb == 0);
+  return GB300_OK;
+}
+
 int generate_pattern(gb300_matrix *A, const gb300_term_batch *t)
 {
   int nv, nloc;
@@ -577,11 +672,16 @@ int generate_pattern(gb300_matrix *A, const gb300_term_batch *t)
   A->hr.clear();
   A->hc.clear();
   A->hv.clear();
-  GB_TRY(build_pattern_from_elements(A, t->n_elems, nloc, B.p_edofs, flag, cplx));
+  bool blocks = false;
+  if(t->kind == GB300_TERM_TET10_ELASTICITY)
+    GB_TRY(node_components_ok(A, t->n_elems, B.p_edofs, &blocks));
+  GB_TRY(build_pattern_from_elements(A, t->n_elems, nloc, B.p_edofs, flag, cplx,
+                                     blocks ? 3 : 1));
   // the elasticity tables number unknowns component by component; the
   // solver checks the block structure itself before relying on it
   A->block3 = (t->kind == GB300_TERM_TET10_ELASTICITY);
   A->block_rows = cplx ? 2 : 1;
+  A->node_blocks = blocks;
   return GB300_OK;
 }
 
@@ -623,8 +723,12 @@ int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t,
                                                      t->p0, B.p_coef3, V, b->d.p);
       break;
     case GB300_TERM_TET10_ELASTICITY:
-      k_tet10_elasticity<<<grid_for(ne, kElWarps), 32 * kElWarps, 0, st>>>(
-        ne, B.p_nodes, B.p_elems, B.p_edofs, B.p_coef, t->p0, t->p1, V, b->d.p);
+      if(A->node_blocks)
+        k_tet10_elasticity<1><<<grid_for(ne, kElWarps), 32 * kElWarps, 0, st>>>(
+          ne, B.p_nodes, B.p_elems, B.p_edofs, B.p_coef, t->p0, t->p1, V, b->d.p);
+      else
+        k_tet10_elasticity<0><<<grid_for(ne, kElWarps), 32 * kElWarps, 0, st>>>(
+          ne, B.p_nodes, B.p_elems, B.p_edofs, B.p_coef, t->p0, t->p1, V, b->d.p);
       break;
     case GB300_TERM_TRI3_MAGNETOSTATIC_NL:
       k_tri3_nl<<<grid_for(ne, 256), 256, 0, st>>>(ne, B.p_nodes, B.p_elems, B.p_edofs,

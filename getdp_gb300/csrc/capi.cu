@@ -634,6 +634,7 @@ int gb300_matrix_set_csr(gb300_matrix *A, long long nnz, const int *rowptr,
   A->pattern_version++;
   A->val32_valid = false;
   A->block3 = false;
+  A->node_blocks = false;
   A->bsr_var32 = A->bsr_var64 = -1;
   A->hr.clear();
   A->hc.clear();

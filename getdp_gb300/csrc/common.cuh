@@ -217,6 +217,9 @@ struct gb300_matrix {
   // three-component system in GetDP's component-major numbering (set by the
   // elasticity Generate hook): the CG may iterate on a 3x3-blocked copy
   bool block3 = false;
+  // the pattern has been verified to hold 3 x 3 node blocks (elasticity
+  // Generate: one search per node pair); reset by every pattern build
+  bool node_blocks = false;
   int bsr_var32 = -1, bsr_var64 = -1;  // tuned SpMV launch shapes (-1: not yet)
   // ILU(0) state, created on demand by the solver
   gb::ilu_data *ilu = nullptr;

@@ -123,23 +123,26 @@ __device__ __forceinline__ int next_pow2(int v)
 // ---------------------------------------------------------------------------
 // rows of the complex (two-harmonic) layout are (2*base + h); the element
 // table holds the harmonic-0 number 2*base of each local DOF
+// rows >= lim are not built from their own adjacency (copies of row
+// r - k lim, see rep below)
 __global__ void k_adj_count(const int *__restrict__ edofs, long long total,
-                            int shift, int *__restrict__ cnt)
+                            int shift, int lim, int *__restrict__ cnt)
 {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if(t >= total) return;
   int d = edofs[t];
-  if(d >= 0) atomicAdd(&cnt[d >> shift], 1);
+  if(d >= 0 && d < lim) atomicAdd(&cnt[d >> shift], 1);
 }
 
 __global__ void k_adj_fill(const int *__restrict__ edofs, long long total,
-                           int nloc, int shift, const long long *__restrict__ ptr,
+                           int nloc, int shift, int lim,
+                           const long long *__restrict__ ptr,
                            int *__restrict__ cursor, int *__restrict__ adj)
 {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if(t >= total) return;
   int d = edofs[t];
-  if(d < 0) return;
+  if(d < 0 || d >= lim) return;
   int b = d >> shift;
   int pos = atomicAdd(&cursor[b], 1);
   adj[ptr[b] + pos] = (int)(t / nloc);
@@ -149,10 +152,12 @@ constexpr int kPatThreads = 128;
 constexpr int kPatCap = 4096;
 
 // one block per row: gather the columns of every element touching the row,
-// sort, count (mode 0) or write (mode 1) the distinct ones
+// sort, count (mode 0) or write (mode 1) the distinct ones; with rep > 1
+// the n rows built are also those of rows r + k n (k < rep), which have the
+// same elements (the components of a vector field's node)
 template <int WRITE>
 __global__ void __launch_bounds__(kPatThreads)
-k_pattern_rows(int n, int nloc, int complex_mode, const int *__restrict__ edofs,
+k_pattern_rows(int n, int rep, int nloc, int complex_mode, const int *__restrict__ edofs,
                const unsigned char *__restrict__ cflag,
                const long long *__restrict__ adj_ptr,
                const int *__restrict__ adj, int *__restrict__ row_cnt,
@@ -172,7 +177,8 @@ k_pattern_rows(int n, int nloc, int complex_mode, const int *__restrict__ edofs,
   if(total > kPatCap) {
     if(threadIdx.x == 0) {
       atomicMax(err, (int)total);
-      if(!WRITE) row_cnt[r] = 0;
+      if(!WRITE)
+        for(int k = 0; k < rep; k++) row_cnt[r + (long long)k * n] = 0;
     }
     return;
   }
@@ -217,23 +223,28 @@ k_pattern_rows(int n, int nloc, int complex_mode, const int *__restrict__ edofs,
     __syncthreads();
     int off = running;
     for(int q = 0; q < w; q++) off += wsum[q];
-    if(WRITE && f) col[rowptr[r] + off + wpre] = s[t];
+    if(WRITE && f)
+      for(int k = 0; k < rep; k++) col[rowptr[r + (long long)k * n] + off + wpre] = s[t];
     int chunk = 0;
     for(int q = 0; q < kPatThreads / 32; q++) chunk += wsum[q];
     running += chunk;
     __syncthreads();
   }
-  if(!WRITE && threadIdx.x == 0) row_cnt[r] = running;
+  if(!WRITE && threadIdx.x == 0)
+    for(int k = 0; k < rep; k++) row_cnt[r + (long long)k * n] = running;
 }
 
 int build_pattern_from_elements(gb300_matrix *A, int ne, int nloc,
                                 const int *d_edofs,
-                                const unsigned char *d_cflag, int complex_mode)
+                                const unsigned char *d_cflag, int complex_mode,
+                                int rep)
 {
   cudaStream_t st = A->ctx->stream;
   int n = A->n;
+  if(rep < 1 || n % rep || complex_mode) rep = 1;
+  const int nb = n / rep;  // rows built; the others are copies
   int shift = complex_mode ? 1 : 0;
-  int nbase = complex_mode ? n / 2 : n;
+  int nbase = complex_mode ? n / 2 : nb;
   long long total = (long long)ne * nloc;
   DevBuf<int> cnt, cursor, adj, err;
   DevBuf<long long> adj_ptr, tmp, rp64;
@@ -245,18 +256,19 @@ int build_pattern_from_elements(gb300_matrix *A, int ne, int nloc,
   GB_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int) * (nbase + 1), st));
   GB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
   k_adj_count<<<grid_for(total, 256), 256, 0, st>>>(d_edofs, total, shift,
-                                                     cnt.p);
+                                                     rep > 1 ? nb : n, cnt.p);
   long long nadj = 0;
   GB_TRY(exclusive_scan(cnt.p, nbase + 1, adj_ptr.p, &nadj, tmp, st));
   GB_CUDA(cudaStreamSynchronize(st));
   GB_TRY(adj.alloc(nadj > 0 ? nadj : 1));
   k_adj_fill<<<grid_for(total, 256), 256, 0, st>>>(d_edofs, total, nloc, shift,
-                                                    adj_ptr.p, cursor.p, adj.p);
+                                                    rep > 1 ? nb : n, adj_ptr.p,
+                                                    cursor.p, adj.p);
   // count pass
   DevBuf<int> row_cnt;
   GB_TRY(row_cnt.alloc(n + 1));
   GB_CUDA(cudaMemsetAsync(row_cnt.p + n, 0, sizeof(int), st));
-  k_pattern_rows<0><<<n, kPatThreads, 0, st>>>(n, nloc, complex_mode, d_edofs,
+  k_pattern_rows<0><<<nb, kPatThreads, 0, st>>>(nb, rep, nloc, complex_mode, d_edofs,
                                                 d_cflag, adj_ptr.p, adj.p,
                                                 row_cnt.p, nullptr, nullptr,
                                                 err.p);
@@ -279,7 +291,7 @@ int build_pattern_from_elements(gb300_matrix *A, int ne, int nloc,
   GB_TRY(A->col.alloc(nnz > 0 ? nnz : 1));
   GB_TRY(A->val.alloc(nnz > 0 ? nnz : 1));
   k_i64_to_i32<<<grid_for(n + 1, 256), 256, 0, st>>>(rp64.p, n + 1, A->rowptr.p);
-  k_pattern_rows<1><<<n, kPatThreads, 0, st>>>(n, nloc, complex_mode, d_edofs,
+  k_pattern_rows<1><<<nb, kPatThreads, 0, st>>>(nb, rep, nloc, complex_mode, d_edofs,
                                                 d_cflag, adj_ptr.p, adj.p,
                                                 nullptr, rp64.p, A->col.p, err.p);
   GB_CUDA(cudaMemsetAsync(A->val.p, 0, sizeof(double) * (nnz > 0 ? nnz : 1), st));
@@ -289,6 +301,7 @@ int build_pattern_from_elements(gb300_matrix *A, int ne, int nloc,
   A->pattern_version++;
   A->val32_valid = false;
   A->block3 = false;
+  A->node_blocks = false;
   A->bsr_var32 = A->bsr_var64 = -1;
   choose_tpr(A);
   GB_CUDA(cudaStreamSynchronize(st));
@@ -447,6 +460,7 @@ int build_csr_from_coo(gb300_matrix *A, long long m, const int *d_r,
   A->pattern_version++;
   A->val32_valid = false;
   A->block3 = false;
+  A->node_blocks = false;
   A->bsr_var32 = A->bsr_var64 = -1;
   choose_tpr(A);
   return GB300_OK;

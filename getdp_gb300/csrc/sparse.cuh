@@ -8,9 +8,11 @@ namespace gb {
 int exclusive_scan(const int *in, long long n, long long *out, long long *total,
                    DevBuf<long long> &tmp, cudaStream_t st);
 void choose_tpr(gb300_matrix *A);
+// rep > 1: rows r + k n/rep (k < rep) have row r's elements (checked by
+// the caller), so only the first n/rep rows are built and copied
 int build_pattern_from_elements(gb300_matrix *A, int ne, int nloc,
                                 const int *d_edofs, const unsigned char *d_cflag,
-                                int complex_mode);
+                                int complex_mode, int rep = 1);
 int build_csr_from_coo(gb300_matrix *A, long long m, const int *d_r,
                        const int *d_c, const double *d_v);
 
