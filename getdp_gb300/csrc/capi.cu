@@ -180,7 +180,7 @@ void gb300_solver_params_default(gb300_solver_params *p)
   p->nb_iter_max = 1000;
   p->stopping_test = 1.e-10;
   p->precision = 0;
-  p->inner_tolerance = 1.e-4;
+  p->inner_tolerance = 0.3;
   p->inner_iter_max = 1000;
 }
 

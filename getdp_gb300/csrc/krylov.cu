@@ -575,12 +575,19 @@ __global__ void k_fold_all(int n, double *__restrict__ x, const float *__restric
   if(i < n) x[i] += (double)x32[i];
 }
 
+// the FP32 residual reduction between two FP64 residual replacements
+static double reliable_delta(const gb300_solver_params *p)
+{
+  double d = p->inner_tolerance;
+  return (d > 0. && d < 1.) ? d : 0.3;
+}
+
 // spmv32(p, q, part, S, st): FP32 q = A p with partial <p, q>;
 // res64(x, b, r, part, flag, st): FP64 r = b - A x with partial ||r||^2
 template <typename SPMV32, typename RES64>
 static int cg_mixed_core(cudaStream_t st, int n, SPMV32 spmv32, RES64 res64,
                          const double *rhs, double *x, double rtol, int maxit,
-                         CgState *hs, Work &W)
+                         double delta, CgState *hs, Work &W)
 {
   float *r32 = (float *)W.vec(0, n * sizeof(float));
   float *p32 = (float *)W.vec(1, n * sizeof(float));
@@ -597,7 +604,7 @@ static int cg_mixed_core(cudaStream_t st, int n, SPMV32 spmv32, RES64 res64,
   k_convert<float, double><<<gl, 256, 0, st>>>(n, rhs, r32);
   k_copy<float><<<gl, 256, 0, st>>>(n, r32, p32);
   dot_part64(n, rhs, rhs, part, st);
-  k_rcg_start<<<1, 256, 0, st>>>(S, part, rtol, maxit, 0.1);
+  k_rcg_start<<<1, 256, 0, st>>>(S, part, rtol, maxit, delta);
   GB_CUDA(cudaGetLastError());
 
   // Main graph: a batch of FP32 iterations (SpMV, step, direction).  When a
@@ -844,7 +851,7 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
           bsr_residual64(B, xx, bb, rr, part, flag, s);
         };
         GB_TRY(cg_mixed_core(st, n4, spmv, res, rhs4, x4, p->stopping_test,
-                             p->nb_iter_max, &hs, W));
+                             p->nb_iter_max, reliable_delta(p), &hs, W));
       }
       from_nodes64(nn, x4, x, st);
     }
@@ -870,7 +877,7 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
         residual64_guarded(A, val, xx, bb, rr, part, flag, s);
       };
       GB_TRY(cg_mixed_core(st, n, spmv, res, rhs, x, p->stopping_test,
-                           p->nb_iter_max, &hs, W));
+                           p->nb_iter_max, reliable_delta(p), &hs, W));
     }
     info->status = hs.status;
     info->iterations = hs.its;

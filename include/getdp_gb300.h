@@ -85,7 +85,9 @@ typedef struct gb300_solver_params {
   double stopping_test;
   /* extensions */
   int precision;          /* Precision: 0 FP64, 1 FP32 inner solves in FP64 refinement */
-  double inner_tolerance; /* Inner_Tolerance: relative reduction per inner solve */
+  double inner_tolerance; /* Inner_Tolerance: mixed CG, reduction of the FP32
+                             residual between two FP64 residual replacements
+                             (default 0.3) */
   int inner_iter_max;     /* Inner_Iter_Max */
 } gb300_solver_params;
 
