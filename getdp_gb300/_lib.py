@@ -114,6 +114,16 @@ SIGNATURES = {
     "gb300_generate_values": (_I, [_P, _P, ctypes.POINTER(TermBatch)]),
     "gb300_generate_values_at": (_I, [_P, _P, ctypes.POINTER(TermBatch), _P]),
     "gb300_solve": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, ctypes.POINTER(SolveInfo)]),
+    "gb300_matrix_set_correction": (_I, [_P, _P, _I]),
+    "gb300_precond_apply": (_I, [_P, ctypes.POINTER(SolverParams), _P, _P]),
+    "gb300_mpnn_param_count": (_I, []),
+    "gb300_mpnn_create": (_I, [_P, ctypes.c_uint, _PP]),
+    "gb300_mpnn_destroy": (_I, [_P]),
+    "gb300_mpnn_set_params": (_I, [_P, _P]),
+    "gb300_mpnn_get_params": (_I, [_P, _P]),
+    "gb300_mpnn_infer": (_I, [_P, _P]),
+    "gb300_mpnn_loss_grad": (_I, [_P, _P, _P, _P, _I, ctypes.POINTER(_D), _P]),
+    "gb300_mpnn_adam_step": (_I, [_P, ctypes.c_float, ctypes.c_float]),
     "gb300_post_elements": (_I, [ctypes.POINTER(TermBatch), _P, _P]),
     "gb300_post_points": (_I, [ctypes.POINTER(TermBatch), _P, _I, _P, _P, _P, _P]),
     "gb300_solve_batch": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, _I,

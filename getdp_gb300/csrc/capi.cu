@@ -750,6 +750,37 @@ int gb300_solve(gb300_matrix *A, const gb300_vector *b,
   return solve(A, b, p, x, info);
 }
 
+int gb300_matrix_set_correction(gb300_matrix *A, const double *values, int on_device)
+{
+  GB_TRY(check(A, "matrix"));
+  GB_TRY(gb300_matrix_assemble(A));
+  if(A->nnz > 0) {
+    GB_TRY(check(values, "values"));
+    GB_TRY(A->corr.alloc(A->nnz));
+    GB_CUDA(cudaMemcpyAsync(A->corr.p, values, sizeof(double) * A->nnz,
+                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                            A->ctx->stream));
+    GB_CUDA(cudaStreamSynchronize(A->ctx->stream));
+  }
+  A->corr_version = A->pattern_version;
+  return GB300_OK;
+}
+
+int gb300_precond_apply(gb300_matrix *A, const gb300_solver_params *p,
+                        const gb300_vector *v, gb300_vector *z)
+{
+  GB_TRY(check(A, "matrix"));
+  GB_TRY(check(p, "params"));
+  GB_TRY(check(v, "v"));
+  GB_TRY(check(z, "z"));
+  GB_TRY(gb300_matrix_assemble(A));
+  if(v->n != A->n || z->n != A->n || v == z) {
+    set_error("preconditioner apply: sizes or aliasing");
+    return GB300_ERR_ARG;
+  }
+  return precond_apply(A, p, v->d.p, z->d.p);
+}
+
 int gb300_post_elements(const gb300_term_batch *t, const gb300_vector *x,
                         double *out)
 {

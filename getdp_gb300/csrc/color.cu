@@ -384,11 +384,78 @@ int gmres_solve_coloured(gb300_matrix *A, const double *val, const double *rhs,
   GB_TRY(rb.alloc(n));
   GB_TRY(yb.alloc(n));
   permute_system(C, A->nnz, val, rhs, B->val.p, rb.p, st);
+  if(correction_valid(A)) {  // the learned correction follows the rows
+    GB_TRY(B->corr.alloc(A->nnz));
+    k_gather_vals<<<grid_for(A->nnz, 256), 256, 0, st>>>(A->nnz, C->src.p, A->corr.p,
+                                                          B->corr.p);
+    B->corr_version = B->pattern_version;
+  }
   GB_CUDA(cudaGetLastError());
   rc = gmres_solve(B, B->val.p, rb.p, yb.p, p, info, W);
   if(rc != GB300_OK) return rc;
   unpermute_solution(C, yb.p, x, st);
   GB_CUDA(cudaGetLastError());
+  return GB300_OK;
+}
+
+// z = M^-1 v for the preconditioner a solve with parameters p would use
+// (ILU(0) in GetDP's order or the multicolour order, plus the learned
+// correction for Preconditioner 20), on A's unscaled values
+int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v,
+                  double *z)
+{
+  cudaStream_t st = A->ctx->stream;
+  const int n = A->n;
+  const bool learned = (p->preconditioner == kPrecondLearned);
+  if(p->preconditioner != 6 && !learned) {
+    set_error("preconditioner apply: Preconditioner %d is not an ILU(0)", p->preconditioner);
+    return GB300_ERR_UNSUPPORTED;
+  }
+  if(learned && !correction_valid(A)) {
+    set_error("Preconditioner %d needs a correction on the matrix pattern", p->preconditioner);
+    return GB300_ERR_ARG;
+  }
+  const bool fp32 = (p->precision != 0);
+  gb300_matrix *M = A;
+  DevBuf<double> vb, zb, t1, t2;
+  DevBuf<float> t32;
+  GB_TRY(t1.alloc(n));
+  GB_TRY(t2.alloc(n));
+  if(fp32) GB_TRY(t32.alloc(n));
+  const double *vin = v;
+  double *zout = z;
+  Colouring *C = nullptr;
+  if(p->renumbering_technique == 1) {
+    const int whole[2] = {0, n};
+    int rc = colour_build(A, 1, whole);
+    if(rc != GB300_OK && rc != GB300_ERR_UNSUPPORTED) return rc;
+    if(rc == GB300_OK) {
+      C = A->mc;
+      M = C->B;
+      GB_TRY(vb.alloc(n));
+      GB_TRY(zb.alloc(n));
+      permute_system(C, A->nnz, A->val.p, v, M->val.p, vb.p, st);
+      if(learned) {
+        GB_TRY(M->corr.alloc(A->nnz));
+        k_gather_vals<<<grid_for(A->nnz, 256), 256, 0, st>>>(A->nnz, C->src.p, A->corr.p,
+                                                              M->corr.p);
+        M->corr_version = M->pattern_version;
+      }
+      vin = vb.p;
+      zout = zb.p;
+    }
+  }
+  int zr = 0;
+  GB_TRY(ilu_factor(M, M->val.p, fp32, &zr));
+  if(zr) {
+    set_error("Zero pivot on line %d in ILU", zr);
+    return GB300_ERR_ZERO_PIVOT;
+  }
+  ilu_apply(M, fp32, vin, zout, fp32 ? t32.p : nullptr, nullptr, st);
+  if(learned) correction_apply(M, M->val.p, vin, zout, t1.p, t2.p, nullptr, st);
+  if(C) unpermute_solution(C, zout, z, st);
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(st));
   return GB300_OK;
 }
 

@@ -229,4 +229,8 @@ struct gb300_matrix {
   gb::Colouring *mc = nullptr;
   // rows per unknown (2: complex system in real form, harmonic-interleaved)
   int block_rows = 1;
+  // learned preconditioner correction on the pattern (valid while
+  // corr_version == pattern_version)
+  gb::DevBuf<double> corr;
+  unsigned corr_version = ~0u;
 };

@@ -662,6 +662,42 @@ __global__ void k_gm_apply_ok(GmState *S, int *ok)
   if(threadIdx.x == 0) *ok = (S->active && S->did_cycle) ? 1 : 0;
 }
 
+bool correction_valid(const gb300_matrix *A)
+{
+  return A->corr_version == A->pattern_version && A->corr.p && A->nnz > 0;
+}
+
+// r1 = v - A z
+__global__ void k_sub_from(int n, const double *__restrict__ v, double *__restrict__ t,
+                           const int *flag)
+{
+  if(flag && !*flag) return;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x)
+    t[i] = v[i] - t[i];
+}
+
+__global__ void k_add_to(int n, const double *__restrict__ t, double *__restrict__ z,
+                         const int *flag)
+{
+  if(flag && !*flag) return;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x)
+    z[i] += t[i];
+}
+
+// z <- z + G (v - A z): the learned correction after the ILU(0) step
+void correction_apply(const gb300_matrix *A, const double *val, const double *v,
+                      double *z, double *t1, double *t2, const int *flag, cudaStream_t st)
+{
+  const int n = A->n;
+  const int g = grid_for(n, 256, kReduceBlocks * 4);
+  spmv_guarded(A, val, z, t1, flag, st);
+  k_sub_from<<<g, 256, 0, st>>>(n, v, t1, flag);
+  spmv_guarded(A, A->corr.p, t1, t2, flag, st);
+  k_add_to<<<g, 256, 0, st>>>(n, t2, z, flag);
+}
+
 int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
                 double *x, const gb300_solver_params *p, gb300_solve_info *info,
                 Work &W)
@@ -679,10 +715,18 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
     set_error("Krylov_Size %d exceeds this backend's maximum %d", m, kMaxKrylov);
     return GB300_ERR_UNSUPPORTED;
   }
-  bool precond = (p->preconditioner == 6);
-  if(p->preconditioner != 0 && p->preconditioner != 6 && p->preconditioner != 8) {
+  // 20: ILU(0) followed by the learned correction on A's pattern
+  const bool learned = (p->preconditioner == kPrecondLearned);
+  bool precond = (p->preconditioner == 6) || learned;
+  if(p->preconditioner != 0 && p->preconditioner != 6 && p->preconditioner != 8 &&
+     !learned) {
     set_error("Preconditioner %d is not supported by this backend", p->preconditioner);
     return GB300_ERR_UNSUPPORTED;
+  }
+  if(learned && !correction_valid(A)) {
+    set_error("Preconditioner %d needs a correction on the matrix pattern "
+              "(gb300_matrix_set_correction)", p->preconditioner);
+    return GB300_ERR_ARG;
   }
   bool fp32 = (p->precision != 0);
   if(precond) {
@@ -705,7 +749,10 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   double *part = (double *)W.vec(6, sizeof(double) * kReduceBlocks * (m + 1));
   GmState *S = (GmState *)W.state(sizeof(GmState));
   int *okflag = (int *)W.vec(7, sizeof(int));
-  if(!V || (flexible && !Z) || !r || !u || !zt || (fp32 && !t32) || !part || !S)
+  double *t1 = learned ? (double *)W.vec(8, sizeof(double) * n) : nullptr;
+  double *t2 = learned ? (double *)W.vec(9, sizeof(double) * n) : nullptr;
+  if(!V || (flexible && !Z) || !r || !u || !zt || (fp32 && !t32) || !part || !S ||
+     (learned && (!t1 || !t2)))
     return GB300_ERR_CUDA;
   GmState h0;
   memset(&h0, 0, sizeof(h0));
@@ -723,6 +770,7 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
       ilu_apply(A, fp32, v, z, t32, flag, st);
     else
       k_cvt<double, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, z, flag);
+    if(learned) correction_apply(A, val, v, z, t1, t2, flag, st);
   };
 
   cudaGraph_t graph;

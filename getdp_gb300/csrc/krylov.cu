@@ -888,11 +888,13 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
     }
   }
   else if(p->algorithm == 8 || p->algorithm == 9 ||
-          (p->algorithm == 1 && p->preconditioner == 6)) {
+          (p->algorithm == 1 && (p->preconditioner == 6 ||
+                                 p->preconditioner == kPrecondLearned))) {
     // Renumbering_Technique 1 (RCMK in Sparskit): this backend's own
     // renumbering, a multicolour ordering, for the ILU(0) solves
     bool used = false;
-    if(p->renumbering_technique == 1 && p->preconditioner == 6) {
+    if(p->renumbering_technique == 1 &&
+       (p->preconditioner == 6 || p->preconditioner == kPrecondLearned)) {
       rc = gmres_solve_coloured(A, val, rhs, x, p, info, W, &used);
       if(rc != GB300_OK) return rc;
     }

@@ -57,6 +57,13 @@ void bsr_spmv_dot64(const Bsr3 &B, const double *p, double *q, double *part,
 void bsr_residual64(const Bsr3 &B, const double *x, const double *b, double *r,
                     double *part, const int *flag, cudaStream_t st);
 
+// Preconditioner 20 (not a Sparskit value): ILU(0), then z += G (v - A z)
+// with G the learned correction on A's pattern (gb300_matrix_set_correction)
+constexpr int kPrecondLearned = 20;
+bool correction_valid(const gb300_matrix *A);
+void correction_apply(const gb300_matrix *A, const double *val, const double *v,
+                      double *z, double *t1, double *t2, const int *flag, cudaStream_t st);
+
 // ILU(0) of A's pattern on the values val (FP64, or FP32 storage), and its
 // application z = M^-1 v guarded by *flag (gmres.cu)
 int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out);

@@ -45,6 +45,8 @@ void ilu_free(ilu_data *d);
 
 int solve(gb300_matrix *A, const gb300_vector *b, const gb300_solver_params *p,
           gb300_vector *x, gb300_solve_info *info);
+int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v,
+                  double *z);
 int post_elements(const gb300_term_batch *t, const gb300_vector *x, double *out);
 int post_points(const gb300_term_batch *t, const gb300_vector *x, int np,
                 const double *xyz, double *field, double *curl, int *elem);

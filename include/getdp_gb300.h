@@ -275,6 +275,41 @@ int gb300_residual_noalloc(gb300_matrix *A, const gb300_vector *x,
                            const gb300_vector *b, gb300_vector *r,
                            double *norm);
 
+/* ---- learned preconditioner ------------------------------------------ */
+/* No counterpart in the reference.  Preconditioner 20 (not a Sparskit
+   value) is ILU(0) followed by a correction z += G (v - A z), G a sparse
+   matrix on A's pattern.  gb300_matrix_set_correction attaches G (values in
+   A's CSR order, host or device pointer); a pattern change drops it. */
+int gb300_matrix_set_correction(gb300_matrix *A, const double *values, int on_device);
+/* z = M^-1 v with the preconditioner the solver would use for p
+   (Preconditioner 6 or 20; Renumbering_Technique selects the ordering) on
+   A's unscaled values. */
+int gb300_precond_apply(gb300_matrix *A, const gb300_solver_params *p,
+                        const gb300_vector *v, gb300_vector *z);
+/* The network that predicts G: 3 message-passing layers of width 32 over the
+   matrix graph, BF16 weights, FP32 accumulation (getdp_gb300/csrc/learned.cu).
+   gb300_mpnn_infer computes G for A and attaches it (set_correction).
+   gb300_mpnn_loss_grad runs the forward and backward passes for one system
+   with the energy-norm loss 1 + (y^T A y - 2 r1^T y) / S, y = G r1, which
+   is (G r1 - e1)^T A (G r1 - e1) / e1^T A e1 for e1 = A^-1 r1 (A symmetric
+   positive definite; r1 = v - A z1, z1 = ILU^-1 v): S = e1^T A e1 when e1
+   (x* - z1 for a solved right-hand side) is given, r1^T diag(A)^-1 r1 for a
+   probe without solution (e1 NULL); it adds the weight gradients to the
+   network's gradient
+   (zeroed first unless accumulate); grad_host (param_count floats) may be
+   NULL.  gb300_mpnn_adam_step applies grad_scale * gradient with Adam. */
+typedef struct gb300_mpnn gb300_mpnn;
+int gb300_mpnn_param_count(void);
+int gb300_mpnn_create(gb300_ctx *ctx, unsigned seed, gb300_mpnn **out);
+int gb300_mpnn_destroy(gb300_mpnn *net);
+int gb300_mpnn_set_params(gb300_mpnn *net, const float *host);
+int gb300_mpnn_get_params(const gb300_mpnn *net, float *host);
+int gb300_mpnn_infer(gb300_mpnn *net, gb300_matrix *A);
+int gb300_mpnn_loss_grad(gb300_mpnn *net, gb300_matrix *A, const gb300_vector *r1,
+                         const gb300_vector *e1, int accumulate, double *loss,
+                         float *grad_host);
+int gb300_mpnn_adam_step(gb300_mpnn *net, float lr, float grad_scale);
+
 /* ---- solve ------------------------------------------------------------ */
 /* LinAlg_Solve -> solve_matrix (Sparskit.cpp:108-634) on the GPU.  A and b
    are not modified (Sparskit scales them in place; here scaling acts on

@@ -1,0 +1,132 @@
+"""The learned correction of the ILU(0) preconditioner: the network's
+hand-written forward and backward kernels against the FP64 oracle
+(oracle/mpnn_port.py), the oracle's gradient against finite differences,
+training on the GPU, and the solve with its fallback.
+
+Tolerances: oracle gradient vs central differences (FP64, no BF16
+rounding): 1e-6 of the largest gradient entry; GPU vs oracle (same BF16
+weights; the GPU accumulates in FP32 with atomics in varying order): loss
+within 1e-5 relative, gradient within 2e-3 of the largest entry.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+from getdp_gb300 import workloads as W
+from oracle import mpnn_port as M
+
+
+def small_system(n=6, seed=5):
+    p = W.nonlinear_2d(n=n, seed=seed)
+    dm = W.dofmap_for(p)
+    ip, ix, dv, b = oracle.assemble(p, dm)
+    return p, dm, ip, ix, dv, b
+
+
+@pytest.mark.parametrize("with_solution", [True, False])
+def test_oracle_gradient_matches_finite_differences(with_solution):
+    oracle.build()
+    _, _, ip, ix, dv, _ = small_system()
+    A = sp.csr_matrix((dv, ix, ip))
+    g = M.graph(ip, ix, dv)
+    rng = np.random.default_rng(3)
+    w = rng.standard_normal(M.NPARAM) * 0.3
+    r1 = rng.standard_normal(g["n"])
+    e1 = rng.standard_normal(g["n"]) if with_solution else None
+    _, grad, _ = M.loss_grad(w, g, r1, e1, A, bf16_weights=False)
+    idx = np.concatenate([rng.choice(M.NPARAM, 40, replace=False),
+                          [M.OFF_CO, M.OFF_BD, M.OFF_WO + 1, M.OFF_WD + 2, M.OFF_WIN]])
+    h = 1e-6
+    for k in idx:
+        wp, wm = w.copy(), w.copy()
+        wp[k] += h
+        wm[k] -= h
+        fd = (M.loss_grad(wp, g, r1, e1, A, bf16_weights=False)[0] -
+              M.loss_grad(wm, g, r1, e1, A, bf16_weights=False)[0]) / (2 * h)
+        assert abs(fd - grad[k]) <= 1e-6 * np.abs(grad).max() + 1e-12, (k, fd, grad[k])
+
+
+def test_bf16_rounding_is_round_to_nearest_even():
+    x = np.array([1.0, 1.00390625, 1.005859375, -2.5, 3.0e-3], np.float32)
+    r = M.bf16(x)
+    u = np.asarray(r, np.float32).view(np.uint32)
+    assert np.all(u & 0xFFFF == 0)
+    assert np.all(np.abs(r - x) <= np.abs(x) * 2.0 ** -8)
+    assert r[1] == 1.0  # the tie 1 + 2^-8 rounds to even
+
+
+# ----------------------------------------------------------------- GPU
+def _gpu():
+    from getdp_gb300 import build
+    build.build()
+    oracle.build()
+    from getdp_gb300 import generate as G
+    from getdp_gb300 import learned as LR
+    from getdp_gb300 import linalg as LA
+    return G, LR, LA
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("with_solution", [True, False])
+def test_gpu_forward_backward_match_oracle(with_solution):
+    G, LR, LA = _gpu()
+    p, dm, ip, ix, dv, b = small_system(n=12, seed=9)
+    A = LA.gMatrix(dm.n_dof)
+    A.set_csr(ip, ix, dv)
+    net = LR.MPNN(seed=4)
+    rng = np.random.default_rng(5)
+    w = (rng.standard_normal(net.n_params) * 0.2).astype(np.float32)
+    net.set_params(w)
+    r1 = rng.standard_normal(dm.n_dof)
+    e1 = rng.standard_normal(dm.n_dof)
+    vr, ve = LA.gVector(dm.n_dof), LA.gVector(dm.n_dof)
+    vr.set(r1)
+    ve.set(e1)
+    loss, grad = net.loss_grad(A, vr, ve if with_solution else None, want_grad=True)
+    g = M.graph(ip, ix, dv)
+    lo, go, _ = M.loss_grad(w.astype(np.float64), g, r1, e1 if with_solution else None,
+                            sp.csr_matrix((dv, ix, ip)))
+    assert abs(loss - lo) <= 1e-5 * abs(lo), (loss, lo)
+    assert np.abs(grad - go).max() <= 2e-3 * np.abs(go).max(), np.abs(grad - go).max()
+
+
+@pytest.mark.gpu
+def test_gpu_training_lowers_held_out_loss_and_solve_falls_back_safely():
+    G, LR, LA = _gpu()
+
+    def system(n, seed):
+        p = W.nonlinear_2d(n=n, seed=seed)
+        dm = W.dofmap_for(p)
+        A, b = G.generate_problem(p, dm)
+        S = LA.LinAlg_CreateSolver(None)
+        for k, v in dict(Algorithm=8, Preconditioner=6, Krylov_Size=50,
+                         Nb_Iter_Max=20000, Renumbering_Technique=1).items():
+            S.set(k, v)
+        S["stopping_test"] = 1e-12
+        x = LA.gVector(dm.n_dof)
+        LA.LinAlg_Solve(A, b, S, x)
+        return A, b, x
+
+    samples = []
+    for s in range(16):
+        A, b, x = system(24, 200 + s)
+        samples.append(LR.make_sample(A, b, x))
+        samples.extend(LR.make_probes(A, 2, seed=300 + s))
+    A, b, x = system(24, 999)
+    held = LR.make_sample(A, b, x)
+    net = LR.MPNN(seed=2)
+    before, _ = net.loss_grad(held.A, held.r1, held.e1)
+    assert abs(before - 1.0) < 1e-9  # the head starts at zero: no correction
+    LR.train(net, samples, epochs=30, lr=3e-3, batch=8)
+    after, _ = net.loss_grad(held.A, held.r1, held.e1)
+    assert after < 0.97, after  # the energy error left by the ILU step shrinks
+    # the solve converges (learned, or the plain fallback when capped) to the
+    # plain solution
+    xs = LA.gVector(A.n)
+    info = LR.solve(A, b, xs, net, stopping_test=1e-12, cap=400)
+    assert info["status"] == 0
+    assert np.linalg.norm(xs.numpy() - x.numpy()) <= 1e-7 * np.linalg.norm(x.numpy())
+    # a cap of one step forces the fallback
+    info = LR.solve(A, b, xs, net, stopping_test=1e-12, cap=1)
+    assert info["preconditioner"].startswith("ilu0") and info["status"] == 0
