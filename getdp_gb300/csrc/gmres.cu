@@ -19,6 +19,8 @@
 // in place of the reference's sequential modified Gram-Schmidt with
 // selective re-orthogonalisation (mgsro, iters.f:3475); both return an
 // orthonormal basis to working precision.
+#include <algorithm>
+
 #include "krylov.cuh"
 
 namespace gb {
@@ -485,14 +487,13 @@ k_gm_dots(int n, int k, const double *__restrict__ V, size_t ldv,
 
 // h[j] = sum of partials (one warp per j); pass 0 stores, pass 1 adds
 __global__ void k_gm_reduce(int k, const double *__restrict__ part, GmState *S,
-                            int pass)
+                            int pass, int nb)
 {
   if(!S->cycle) return;
   int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for(int j = w; j < k; j += blockDim.x / 32) {
     double v = 0.;
-    for(int b = lane; b < kReduceBlocks; b += 32)
-      v += part[(size_t)j * kReduceBlocks + b];
+    for(int b = lane; b < nb; b += 32) v += part[(size_t)j * kReduceBlocks + b];
     v = warp_sum(v);
     if(lane == 0) {
       if(pass == 0)
@@ -532,11 +533,12 @@ k_gm_update(int n, int k, const double *__restrict__ V, size_t ldv,
 }
 
 // end of one Arnoldi step: h(k+1,k), Givens rotations, stopping test
-__global__ void k_gm_step(int k, int m, GmState *S, const double *__restrict__ part)
+__global__ void k_gm_step(int k, int m, GmState *S, const double *__restrict__ part,
+                          int nb)
 {
   if(!S->cycle) return;
   double rr = 0.;
-  for(int i = threadIdx.x; i < kReduceBlocks; i += blockDim.x) rr += part[i];
+  for(int i = threadIdx.x; i < nb; i += blockDim.x) rr += part[i];
   rr = block_sum<double, 256>(rr);
   if(threadIdx.x) return;
   S->its += 1;
@@ -765,6 +767,10 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   GB_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));  // sol = 0
 
   int gs = grid_for(n, 256, kReduceBlocks * 4);
+  // partial-sum blocks of the Arnoldi dot products: one per SM at least,
+  // one per 2048 rows up to kReduceBlocks (small systems keep the
+  // one-block reductions short); fixed for a given n, so deterministic
+  const int nb = std::min(kReduceBlocks, std::max(152, (n + 2047) / 2048));
   auto precond_apply = [&](const double *v, double *z, const int *flag) {
     if(precond)
       ilu_apply(A, fp32, v, z, t32, flag, st);
@@ -786,13 +792,13 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
     double *z = flexible ? Z + (size_t)(k - 1) * ldv : zt;
     precond_apply(vk, z, cycle_flag(S));
     spmv_guarded(A, val, z, w, &S->cycle, st);
-    k_gm_dots<<<kReduceBlocks, 256, 0, st>>>(n, k, V, ldv, w, part, S);
-    k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 0);
-    k_gm_update<0><<<kReduceBlocks, 256, 0, st>>>(n, k, V, ldv, w, part, S, 0);
-    k_gm_dots<<<kReduceBlocks, 256, 0, st>>>(n, k, V, ldv, w, part, S);
-    k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 1);
-    k_gm_update<1><<<kReduceBlocks, 256, 0, st>>>(n, k, V, ldv, w, part, S, 1);
-    k_gm_step<<<1, 256, 0, st>>>(k, m, S, part);
+    k_gm_dots<<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S);
+    k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 0, nb);
+    k_gm_update<0><<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S, 0);
+    k_gm_dots<<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S);
+    k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 1, nb);
+    k_gm_update<1><<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S, 1);
+    k_gm_step<<<1, 256, 0, st>>>(k, m, S, part, nb);
     k_gm_scale_next<<<gs, 256, 0, st>>>(n, S, w, k);
   }
   k_gm_solve_small<<<1, 32, 0, st>>>(S);
