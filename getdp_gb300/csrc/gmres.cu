@@ -265,13 +265,15 @@ __global__ void __launch_bounds__(kNarrowThreads)
 k_levels_narrow(int l0, int l1, const int *__restrict__ lptr,
                 const int *__restrict__ rows, const int *__restrict__ rowptr,
                 const int *__restrict__ col, const int *__restrict__ diag,
-                T *lu, T *inv, T *x, int *zero_row, const int *flag)
+                T *lu, T *inv, T *x, int *zero_row, const int *flag,
+                const unsigned char *__restrict__ rmask)
 {
   if(flag && !*flag) return;
   for(int l = l0; l < l1; l++) {
     int a = lptr[l], b = lptr[l + 1];
     for(int t = a + threadIdx.x; t < b; t += blockDim.x) {
       int i = rows[t];
+      if(MODE != 0 && rmask && !rmask[i]) continue;
       if(MODE == 0)
         row_fact<T>(i, rowptr, col, diag, lu, inv, zero_row);
       else if(MODE == 1)
@@ -288,12 +290,13 @@ __global__ void __launch_bounds__(256)
 k_level_wide(int r0, int width, const int *__restrict__ rows,
              const int *__restrict__ rowptr, const int *__restrict__ col,
              const int *__restrict__ diag, T *lu, T *inv, T *x, int *zero_row,
-             const int *flag)
+             const int *flag, const unsigned char *__restrict__ rmask)
 {
   if(flag && !*flag) return;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if(t >= width) return;
   int i = rows[r0 + t];
+  if(MODE != 0 && rmask && !rmask[i]) return;
   if(MODE == 0)
     row_fact<T>(i, rowptr, col, diag, lu, inv, zero_row);
   else if(MODE == 1)
@@ -302,9 +305,12 @@ k_level_wide(int r0, int width, const int *__restrict__ rows,
     row_bwd<T>(i, rowptr, col, diag, lu, inv, x);
 }
 
+// rmask (sweeps only): rows with rmask[i] == 0 are skipped (the rows of
+// systems of a batch that have stopped)
 template <int MODE, typename T>
 static void run_levels(const gb300_matrix *A, const ilu_data *L, T *lu, T *inv,
-                       T *x, int *zero_row, const int *flag, cudaStream_t st)
+                       T *x, int *zero_row, const int *flag, cudaStream_t st,
+                       const unsigned char *rmask = nullptr)
 {
   bool upper = (MODE == 2);
   const std::vector<Segment> &seg = upper ? L->useg : L->lseg;
@@ -314,11 +320,11 @@ static void run_levels(const gb300_matrix *A, const ilu_data *L, T *lu, T *inv,
     if(s.narrow)
       k_levels_narrow<MODE, T><<<1, kNarrowThreads, 0, st>>>(
         s.l0, s.l1, lptr, rows, A->rowptr.p, A->col.p, L->diag.p, lu, inv, x,
-        zero_row, flag);
+        zero_row, flag, rmask);
     else
       k_level_wide<MODE, T><<<grid_for(s.width, 256), 256, 0, st>>>(
         s.r0, s.width, rows, A->rowptr.p, A->col.p, L->diag.p, lu, inv, x,
-        zero_row, flag);
+        zero_row, flag, rmask);
   }
 }
 
@@ -368,7 +374,8 @@ int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out)
 
 // z = M^-1 v for the ILU(0) factor (double or float work precision)
 void ilu_apply(const gb300_matrix *A, bool fp32, const double *v, double *z,
-               float *t32, const int *flag, cudaStream_t st)
+               float *t32, const int *flag, cudaStream_t st,
+               const unsigned char *rmask)
 {
   const ilu_data *L = A->ilu;
   int n = A->n;
@@ -376,16 +383,16 @@ void ilu_apply(const gb300_matrix *A, bool fp32, const double *v, double *z,
     if(v != z)
       k_cvt<double, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, z, flag);
     run_levels<1, double>(A, L, (double *)L->lu64.p, (double *)L->inv64.p, z,
-                          nullptr, flag, st);
+                          nullptr, flag, st, rmask);
     run_levels<2, double>(A, L, (double *)L->lu64.p, (double *)L->inv64.p, z,
-                          nullptr, flag, st);
+                          nullptr, flag, st, rmask);
   }
   else {
     k_cvt<float, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, t32, flag);
     run_levels<1, float>(A, L, (float *)L->lu32.p, (float *)L->inv32.p, t32,
-                         nullptr, flag, st);
+                         nullptr, flag, st, rmask);
     run_levels<2, float>(A, L, (float *)L->lu32.p, (float *)L->inv32.p, t32,
-                         nullptr, flag, st);
+                         nullptr, flag, st, rmask);
     k_cvt<double, float><<<grid_for(n, 256), 256, 0, st>>>(n, t32, z, flag);
   }
 }

@@ -374,6 +374,17 @@ __global__ void k_b_after(int nsys, BView V)
   }
 }
 
+// rows of the systems whose preconditioner is due: in a cycle (WHICH 0),
+// or with a solution update due (WHICH 1)
+__global__ void k_b_rowmask(Chunks C, BView V, int which, unsigned char *__restrict__ mask)
+{
+  for(int c = blockIdx.x; c < C.n; c += gridDim.x) {
+    const BState &S = V.S[C.sys[c]];
+    unsigned char on = which == 0 ? (S.cycle != 0) : (S.active && S.did_cycle);
+    for(int i = C.r0[c] + threadIdx.x; i < C.r1[c]; i += blockDim.x) mask[i] = on;
+  }
+}
+
 __global__ void k_b_copy(int n, const double *__restrict__ v, double *__restrict__ z,
                          const int *flag)
 {
@@ -515,9 +526,14 @@ int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
   const int gchunks = grid_for(nch, 1, kReduceBlocks);
   const int gsys = grid_for(nsys, 128);
   const int gwarp = grid_for(nsys, 8);  // 8 warps per 256-thread block
-  auto precond_apply = [&](const double *v, double *z, const int *flag) {
-    if(precond)
-      ilu_apply(A, fp32, v, z, t32, flag, st);
+  DevBuf<unsigned char> rmask;
+  GB_TRY(rmask.alloc(n > 0 ? n : 1));
+  // the sweeps visit only the rows of systems still iterating
+  auto precond_apply = [&](const double *v, double *z, const int *flag, int which) {
+    if(precond) {
+      k_b_rowmask<<<gchunks, kBThreads, 0, st>>>(C, V, which, rmask.p);
+      ilu_apply(A, fp32, v, z, t32, flag, st, rmask.p);
+    }
     else
       k_b_copy<<<grid_for(n, 256, kReduceBlocks * 4), 256, 0, st>>>(n, v, z, flag);
   };
@@ -534,7 +550,7 @@ int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
     double *vk = Vb + (size_t)(k - 1) * ldv;
     double *w = Vb + (size_t)k * ldv;
     double *z = flexible ? Z + (size_t)(k - 1) * ldv : zt;
-    precond_apply(vk, z, flags.p);
+    precond_apply(vk, z, flags.p, 0);
     k_b_spmv<4><<<gchunks, kBThreads, 0, st>>>(C, A->rowptr.p, A->col.p, val, z, w, V);
     k_b_dots<<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, part, V);
     k_b_reduce<<<gwarp, 256, 0, st>>>(nsys, k, C, part, V, 0);
@@ -552,7 +568,7 @@ int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
     k_b_combine<1><<<gchunks, kBThreads, 0, st>>>(C, Z, ldv, x, V);
   else {
     k_b_combine<0><<<gchunks, kBThreads, 0, st>>>(C, Vb, ldv, u, V);
-    precond_apply(u, zt, flags.p + 2);
+    precond_apply(u, zt, flags.p + 2, 1);
     k_b_addto<<<gchunks, kBThreads, 0, st>>>(C, zt, x, V);
   }
   k_b_after<<<gsys, 128, 0, st>>>(nsys, V);

@@ -67,8 +67,10 @@ void correction_apply(const gb300_matrix *A, const double *val, const double *v,
 // ILU(0) of A's pattern on the values val (FP64, or FP32 storage), and its
 // application z = M^-1 v guarded by *flag (gmres.cu)
 int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out);
+// rmask (optional): rows with rmask[i] == 0 are left out of the sweeps
 void ilu_apply(const gb300_matrix *A, bool fp32, const double *v, double *z,
-               float *t32, const int *flag, cudaStream_t st);
+               float *t32, const int *flag, cudaStream_t st,
+               const unsigned char *rmask = nullptr);
 
 // the Givens rotation of iters.f's givens (3235-3273): zeroes y against x;
 // x becomes the norm, (c, s) the rotation
