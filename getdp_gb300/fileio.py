@@ -1,0 +1,159 @@
+"""The on-disk formats either side of the path: Gmsh MSH 2.2 meshes in
+(GetDP's reader: GeoData.cpp, Geo_ReadFileWithGmsh) and GetDP .res solution
+files out (DofData.cpp:631-767, Dof_WriteFileRES0 / Dof_WriteFileRES, read
+back by Dof_ReadFileRES).
+
+Parsing is vectorised (numpy) so that a million-element mesh loads in well
+under a second; the .res writer produces what GetDP's own reader accepts
+(the reference's post-processing runs on it, tests/test_fileio.py).
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+# Gmsh element type -> nodes per element (the types GetDP's examples use)
+MSH_NODES = {1: 2, 2: 3, 3: 4, 4: 4, 5: 8, 6: 6, 7: 5, 8: 3, 9: 6, 11: 10, 15: 1}
+
+
+@dataclasses.dataclass
+class MshData:
+    """Nodes (with their Gmsh numbers) and elements grouped by type:
+    elements[type] = (numbers, physical tags, elementary tags, 0-based node
+    indices)."""
+
+    node_numbers: np.ndarray
+    nodes: np.ndarray
+    elements: dict
+
+
+def _section(data: bytes, name: bytes):
+    a = data.index(b"$" + name)
+    a = data.index(b"\n", a) + 1
+    b = data.index(b"$End" + name, a)
+    return a, b
+
+
+def read_msh22(path: str) -> MshData:
+    """Gmsh MSH 2.2, ASCII or binary (little-endian)."""
+    with open(path, "rb") as f:
+        data = f.read()
+    a, b = _section(data, b"MeshFormat")
+    head = data[a:b].split(b"\n")[0].split()
+    if not head[0].startswith(b"2"):
+        raise ValueError(f"{path}: MSH format {head[0].decode()} (2.x expected)")
+    binary = int(head[1]) == 1
+    a, b = _section(data, b"Nodes")
+    nl = data.index(b"\n", a)
+    nn = int(data[a:nl])
+    if binary:
+        rec = np.dtype([("num", "<i4"), ("xyz", "<f8", 3)])
+        arr = np.frombuffer(data, rec, count=nn, offset=nl + 1)
+        numbers, xyz = arr["num"].astype(np.int64), arr["xyz"].astype(np.float64)
+    else:
+        vals = np.array(data[nl + 1:b].split(), dtype=np.float64).reshape(nn, 4)
+        numbers, xyz = vals[:, 0].astype(np.int64), vals[:, 1:].copy()
+    # node number -> row
+    lookup = np.full(int(numbers.max()) + 1 if nn else 1, -1, np.int64)
+    lookup[numbers] = np.arange(nn)
+    a, b = _section(data, b"Elements")
+    nl = data.index(b"\n", a)
+    ne = int(data[a:nl])
+    groups = {}
+    if binary:
+        off = nl + 1
+        done = 0
+        while done < ne:
+            t, count, ntags = np.frombuffer(data, "<i4", 3, off)
+            off += 12
+            npe = MSH_NODES[int(t)]
+            rec = np.frombuffer(data, "<i4", count * (1 + ntags + npe), off)
+            off += 4 * rec.size
+            rec = rec.reshape(count, 1 + ntags + npe)
+            groups.setdefault(int(t), []).append((rec[:, 0], rec[:, 1:1 + ntags],
+                                                  rec[:, 1 + ntags:]))
+            done += count
+    else:
+        # all numbers of the section, then runs of records of one (type,
+        # tag count) taken a whole block at a time
+        tok = np.array(data[nl + 1:b].split(), dtype=np.int64)
+        p, done = 0, 0
+        while done < ne:
+            t, ntags = int(tok[p + 1]), int(tok[p + 2])
+            rl = 3 + ntags + MSH_NODES[t]
+            left = (len(tok) - p) // rl
+            block = tok[p:p + left * rl].reshape(left, rl)
+            same = (block[:, 1] == t) & (block[:, 2] == ntags)
+            cnt = int(np.argmin(same)) if not same.all() else left
+            cnt = min(cnt, ne - done)
+            m = block[:cnt]
+            groups.setdefault(t, []).append((m[:, 0], m[:, 3:3 + ntags], m[:, 3 + ntags:]))
+            p += cnt * rl
+            done += cnt
+    elements = {}
+    for t, parts in groups.items():
+        num = np.concatenate([p[0] for p in parts]).astype(np.int64)
+        tags = [p[1] for p in parts]
+        width = max(x.shape[1] for x in tags)
+        tags = np.concatenate([np.pad(x, ((0, 0), (0, width - x.shape[1]))) for x in tags])
+        conn = lookup[np.concatenate([p[2] for p in parts]).astype(np.int64)]
+        if (conn < 0).any():
+            raise ValueError(f"{path}: an element refers to an unknown node")
+        phys = tags[:, 0] if width > 0 else np.zeros(len(num), np.int64)
+        elem = tags[:, 1] if width > 1 else np.zeros(len(num), np.int64)
+        order = np.argsort(num, kind="stable")  # GetDP sorts elements by number
+        elements[t] = (num[order], phys[order], elem[order], conn[order].astype(np.int32))
+    return MshData(numbers, xyz, elements)
+
+
+def write_res(path: str, x: np.ndarray, binary: bool = True, dofdata: int = 0,
+              time: float = 0.0, time_imag: float = 0.0, step: int = 0,
+              append: bool = False) -> None:
+    """A GetDP .res file holding solution vector x of DofData `dofdata`
+    (Dof_WriteFileRES0 header, then one $Solution block as
+    Dof_WriteFileRES writes it)."""
+    x = np.ascontiguousarray(x, np.float64)
+    mode = "ab" if append else "wb"
+    with open(path, mode) as f:
+        if not append:
+            f.write(("$ResFormat /* getdp-gb300, %s */\n1.1 %d\n$EndResFormat\n"
+                     % ("binary" if binary else "ascii", 1 if binary else 0)).encode())
+        f.write(("$Solution  /* DofData #%d */\n%d %.16g %.16g %d\n"
+                 % (dofdata, dofdata, time, time_imag, step)).encode())
+        if binary:
+            f.write(x.tobytes())
+            f.write(b"\n")
+        else:
+            f.write("".join("%.16g\n" % v for v in x).encode())
+        f.write(b"$EndSolution\n")
+
+
+def read_res(path: str, n: int) -> list:
+    """Every $Solution block of a .res file: (dofdata, time, time_imag, step,
+    values[n])."""
+    with open(path, "rb") as f:
+        data = f.read()
+    a, b = _section(data, b"ResFormat")
+    version, fmt = data[a:b].split()[:2]
+    binary = int(fmt) == 1
+    out = []
+    pos = 0
+    while True:
+        k = data.find(b"$Solution", pos)
+        if k < 0:
+            break
+        k = data.index(b"\n", k) + 1
+        e = data.index(b"\n", k)
+        h = data[k:e].split()
+        k = e + 1
+        if binary:
+            vals = np.frombuffer(data, np.float64, n, k).copy()
+            k += 8 * n
+        else:
+            end = data.index(b"$EndSolution", k)
+            vals = np.array(data[k:end].split(), dtype=np.float64)[:n]
+            k = end
+        out.append((int(h[0]), float(h[1]), float(h[2]), int(h[3]), vals))
+        pos = data.index(b"$EndSolution", k) + 12
+    return out

@@ -1,0 +1,114 @@
+"""MSH 2.2 reading and .res writing (the formats on either side of the
+path): round trips, the reference's own example mesh, and the reference's
+post-processing reading a .res file written here."""
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+import pytest
+
+from getdp_gb300 import fileio as FIO
+from getdp_gb300 import workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = os.path.join(ROOT, "oracle", "_ref", "getdp_ilu64")
+GETDP_SRC = "/root/reference"
+
+
+@pytest.mark.parametrize("p", [W.magnetostatics_2d(n=9, seed=2), W.curlcurl_edge(n=3, seed=1),
+                               W.elasticity_p2(n=2, seed=1)],
+                         ids=["tri3", "tet4", "tet10"])
+def test_msh_round_trip(p, tmp_path):
+    path = str(tmp_path / "m.msh")
+    W.write_msh22(p.mesh, path)
+    d = FIO.read_msh22(path)
+    assert np.array_equal(d.nodes, p.mesh.nodes)
+    assert np.array_equal(d.node_numbers, np.arange(1, p.mesh.n_nodes + 1))
+    tv = W._MSH_TYPE[p.mesh.kind]
+    num, phys, _, conn = d.elements[tv]
+    assert np.array_equal(conn, p.mesh.elems)
+    assert np.array_equal(phys, p.mesh.region)
+    tb = W._MSH_TYPE[p.mesh.bnd_kind]
+    assert np.array_equal(d.elements[tb][3], p.mesh.bnd)
+
+
+def test_msh_binary(tmp_path):
+    # a binary file written here in the MSH 2.2 binary layout
+    p = W.magnetostatics_2d(n=5, seed=3)
+    m = p.mesh
+    path = str(tmp_path / "b.msh")
+    with open(path, "wb") as f:
+        f.write(b"$MeshFormat\n2.2 1 8\n")
+        f.write(np.array([1], "<i4").tobytes() + b"\n$EndMeshFormat\n$Nodes\n")
+        f.write(f"{m.n_nodes}\n".encode())
+        rec = np.zeros(m.n_nodes, np.dtype([("num", "<i4"), ("xyz", "<f8", 3)]))
+        rec["num"] = np.arange(1, m.n_nodes + 1)
+        rec["xyz"] = m.nodes
+        f.write(rec.tobytes() + b"\n$EndNodes\n$Elements\n")
+        f.write(f"{m.n_elems}\n".encode())
+        f.write(np.array([2, m.n_elems, 2], "<i4").tobytes())
+        body = np.concatenate([np.arange(1, m.n_elems + 1)[:, None], m.region[:, None],
+                               m.region[:, None], m.elems + 1], 1).astype("<i4")
+        f.write(body.tobytes() + b"\n$EndElements\n")
+    d = FIO.read_msh22(path)
+    assert np.array_equal(d.nodes, m.nodes)
+    assert np.array_equal(d.elements[2][3], m.elems)
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(GETDP_SRC, "examples", "magnet.msh")),
+                    reason="reference example not present")
+def test_reads_reference_example_mesh():
+    d = FIO.read_msh22(os.path.join(GETDP_SRC, "examples", "magnet.msh"))
+    assert d.nodes.shape[1] == 3 and len(d.nodes) > 0
+    total = sum(len(v[0]) for v in d.elements.values())
+    with open(os.path.join(GETDP_SRC, "examples", "magnet.msh"), "rb") as f:
+        data = f.read()
+    a = data.index(b"$Elements")
+    assert total == int(data[a:].split(b"\n")[1])
+
+
+@pytest.mark.parametrize("binary", [True, False])
+def test_res_round_trip(binary, tmp_path):
+    x = np.random.default_rng(1).standard_normal(37)
+    path = str(tmp_path / "s.res")
+    FIO.write_res(path, x, binary=binary)
+    FIO.write_res(path, 2 * x, binary=binary, step=1, time=0.5, append=True)
+    sols = FIO.read_res(path, len(x))
+    assert len(sols) == 2
+    if binary:
+        assert np.array_equal(sols[0][4], x) and np.array_equal(sols[1][4], 2 * x)
+    else:  # GetDP prints %.16g: one unit in the 17th digit may differ
+        assert np.allclose(sols[0][4], x, rtol=1e-15, atol=0)
+        assert np.allclose(sols[1][4], 2 * x, rtol=1e-15, atol=0)
+    assert sols[1][1] == 0.5 and sols[1][3] == 1
+
+
+@pytest.mark.skipif(not os.path.exists(REF), reason="reference binary not built")
+@pytest.mark.parametrize("binary", [True, False])
+def test_reference_post_processing_reads_our_res(binary):
+    # the reference prints the same curl values from our .res as from its own
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from make_post_golden import parse_table
+    d = dict(np.load(os.path.join(ROOT, "tests", "golden", "post_ms2d_n8.npz")))
+    p = W.magnetostatics_2d(n=8, seed=11)
+    with tempfile.TemporaryDirectory() as tmp:
+        W.write_pro(p, os.path.join(tmp, "p.pro"))
+        with open(os.path.join(tmp, "p.pro"), "a") as f:
+            f.write(W.post_text(p, []))
+        W.write_msh22(p.mesh, os.path.join(tmp, "p.msh"))
+        FIO.write_res(os.path.join(tmp, "ours.res"), d["x"], binary=binary)
+        r = subprocess.run([REF, "p.pro", "-pre", "R", "-msh", "p.msh", "-pos", "Map",
+                            "-res", "ours.res", "-v", "2"], cwd=tmp,
+                           stdin=subprocess.DEVNULL, capture_output=True, text=True,
+                           timeout=300)
+        out = os.path.join(tmp, "post_elem.txt")
+        assert os.path.exists(out), r.stdout[-2000:] + r.stderr[-2000:]
+        _, _, vals = parse_table(out, 3, 9)
+    got = vals.reshape(-1, 1, 3, 3)
+    if binary:
+        assert np.array_equal(got, d["elem_vals"])
+    else:  # the solution went through %.16g
+        assert np.abs(got - d["elem_vals"]).max() <= 1e-14 * np.abs(d["elem_vals"]).max()
