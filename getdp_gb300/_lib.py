@@ -114,6 +114,12 @@ SIGNATURES = {
     "gb300_generate_values": (_I, [_P, _P, ctypes.POINTER(TermBatch)]),
     "gb300_generate_values_at": (_I, [_P, _P, ctypes.POINTER(TermBatch), _P]),
     "gb300_solve": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, ctypes.POINTER(SolveInfo)]),
+    "gb300_msh_read": (_I, [ctypes.c_char_p, _PP]),
+    "gb300_msh_free": (_I, [_P]),
+    "gb300_msh_nodes": (_I, [_P, ctypes.POINTER(_LL), _PP, _PP]),
+    "gb300_msh_group_count": (_I, [_P, ctypes.POINTER(_I)]),
+    "gb300_msh_group": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_LL),
+                             ctypes.POINTER(_I), ctypes.POINTER(_I), _PP, _PP, _PP]),
     "gb300_matrix_set_correction": (_I, [_P, _P, _I]),
     "gb300_precond_apply": (_I, [_P, ctypes.POINTER(SolverParams), _P, _P]),
     "gb300_mpnn_param_count": (_I, []),

@@ -36,7 +36,49 @@ def _section(data: bytes, name: bytes):
 
 
 def read_msh22(path: str) -> MshData:
-    """Gmsh MSH 2.2, ASCII or binary (little-endian)."""
+    """Gmsh MSH 2.2, ASCII or binary (little-endian), with the library's
+    native parser (gb300_msh_read); read_msh22_numpy is the same in numpy."""
+    import ctypes
+    from . import _lib
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    _lib.check(L.gb300_msh_read(path.encode(), ctypes.byref(h)))
+    try:
+        n = ctypes.c_longlong()
+        pn, px = ctypes.c_void_p(), ctypes.c_void_p()
+        _lib.check(L.gb300_msh_nodes(h, ctypes.byref(n), ctypes.byref(pn), ctypes.byref(px)))
+        nn = n.value
+
+        def arr(ptr, dtype, count):
+            if count == 0:
+                return np.zeros(0, dtype)
+            return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(
+                np.ctypeslib.as_ctypes_type(dtype))), shape=(count,)).copy()
+
+        numbers = arr(pn.value, np.int64, nn)
+        xyz = arr(px.value, np.float64, 3 * nn).reshape(nn, 3)
+        cnt = ctypes.c_int()
+        _lib.check(L.gb300_msh_group_count(h, ctypes.byref(cnt)))
+        groups = {}
+        for g in range(cnt.value):
+            t, ne, nt, npe = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
+            p1, p2, p3 = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+            _lib.check(L.gb300_msh_group(h, g, ctypes.byref(t), ctypes.byref(ne),
+                                         ctypes.byref(nt), ctypes.byref(npe),
+                                         ctypes.byref(p1), ctypes.byref(p2),
+                                         ctypes.byref(p3)))
+            k = ne.value
+            groups.setdefault(t.value, []).append(
+                (arr(p1.value, np.int64, k),
+                 arr(p2.value, np.int32, k * nt.value).reshape(k, nt.value),
+                 arr(p3.value, np.int64, k * npe.value).reshape(k, npe.value)))
+    finally:
+        L.gb300_msh_free(h)
+    return _assemble(path, numbers, xyz, groups)
+
+
+def read_msh22_numpy(path: str) -> MshData:
+    """Gmsh MSH 2.2, ASCII or binary (little-endian), parsed with numpy."""
     with open(path, "rb") as f:
         data = f.read()
     a, b = _section(data, b"MeshFormat")
@@ -54,9 +96,6 @@ def read_msh22(path: str) -> MshData:
     else:
         vals = np.array(data[nl + 1:b].split(), dtype=np.float64).reshape(nn, 4)
         numbers, xyz = vals[:, 0].astype(np.int64), vals[:, 1:].copy()
-    # node number -> row
-    lookup = np.full(int(numbers.max()) + 1 if nn else 1, -1, np.int64)
-    lookup[numbers] = np.arange(nn)
     a, b = _section(data, b"Elements")
     nl = data.index(b"\n", a)
     ne = int(data[a:nl])
@@ -91,6 +130,13 @@ def read_msh22(path: str) -> MshData:
             groups.setdefault(t, []).append((m[:, 0], m[:, 3:3 + ntags], m[:, 3 + ntags:]))
             p += cnt * rl
             done += cnt
+    return _assemble(path, numbers, xyz, groups)
+
+
+def _assemble(path, numbers, xyz, groups) -> MshData:
+    nn = len(numbers)
+    lookup = np.full(int(numbers.max()) + 1 if nn else 1, -1, np.int64)
+    lookup[numbers] = np.arange(nn)
     elements = {}
     for t, parts in groups.items():
         num = np.concatenate([p[0] for p in parts]).astype(np.int64)

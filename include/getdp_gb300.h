@@ -248,6 +248,22 @@ int gb300_post_elements(const gb300_term_batch *t, const gb300_vector *x,
 int gb300_post_points(const gb300_term_batch *t, const gb300_vector *x, int npts,
                       const double *xyz, double *field, double *curl, int *elem);
 
+/* ---- mesh input (Gmsh MSH 2.2) ----------------------------------------- */
+/* The mesh file GetDP reads (Geo_ReadFileWithGmsh, GeoData.cpp), parsed on
+   the host at memory speed, ASCII or binary: nodes with their Gmsh numbers,
+   and elements grouped by (Gmsh type, tag count) in file order with their
+   numbers, tags (physical, elementary, ...) and Gmsh node numbers.  The
+   pointers returned stay valid until gb300_msh_free. */
+typedef struct gb300_msh gb300_msh;
+int gb300_msh_read(const char *path, gb300_msh **out);
+int gb300_msh_free(gb300_msh *m);
+int gb300_msh_nodes(const gb300_msh *m, long long *n, const long long **numbers,
+                    const double **xyz);
+int gb300_msh_group_count(const gb300_msh *m, int *count);
+int gb300_msh_group(const gb300_msh *m, int g, int *type, long long *n_elems,
+                    int *n_tags, int *nodes_per_elem, const long long **numbers,
+                    const int **tags, const long long **nodes);
+
 /* ---- measurement ---------------------------------------------------- */
 /* CUDA events on the context's stream (slots 0..15), for timing calls
    made through this library on the device. */

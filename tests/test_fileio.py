@@ -21,10 +21,11 @@ GETDP_SRC = "/root/reference"
 @pytest.mark.parametrize("p", [W.magnetostatics_2d(n=9, seed=2), W.curlcurl_edge(n=3, seed=1),
                                W.elasticity_p2(n=2, seed=1)],
                          ids=["tri3", "tet4", "tet10"])
-def test_msh_round_trip(p, tmp_path):
+@pytest.mark.parametrize("reader", ["native", "numpy"])
+def test_msh_round_trip(p, reader, tmp_path):
     path = str(tmp_path / "m.msh")
     W.write_msh22(p.mesh, path)
-    d = FIO.read_msh22(path)
+    d = FIO.read_msh22(path) if reader == "native" else FIO.read_msh22_numpy(path)
     assert np.array_equal(d.nodes, p.mesh.nodes)
     assert np.array_equal(d.node_numbers, np.arange(1, p.mesh.n_nodes + 1))
     tv = W._MSH_TYPE[p.mesh.kind]
@@ -53,9 +54,11 @@ def test_msh_binary(tmp_path):
         body = np.concatenate([np.arange(1, m.n_elems + 1)[:, None], m.region[:, None],
                                m.region[:, None], m.elems + 1], 1).astype("<i4")
         f.write(body.tobytes() + b"\n$EndElements\n")
-    d = FIO.read_msh22(path)
-    assert np.array_equal(d.nodes, m.nodes)
-    assert np.array_equal(d.elements[2][3], m.elems)
+    for rd in (FIO.read_msh22, FIO.read_msh22_numpy):
+        d = rd(path)
+        assert np.array_equal(d.nodes, m.nodes)
+        assert np.array_equal(d.elements[2][3], m.elems)
+        assert np.array_equal(d.elements[2][1], m.region)
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(GETDP_SRC, "examples", "magnet.msh")),
