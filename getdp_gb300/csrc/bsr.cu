@@ -201,7 +201,7 @@ k_bsr_spmv(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
   if(flag && !*flag) return;
   const int rows_per_block = 256 / LPR;
   int lane = threadIdx.x % LPR, sub = threadIdx.x / LPR;
-  double red = 0.;
+  typename Acc<T>::type red = 0;
   for(long long a0 = (long long)blockIdx.x * rows_per_block; a0 < nn;
       a0 += (long long)gridDim.x * rows_per_block) {
     long long a = a0 + sub;
@@ -230,7 +230,7 @@ k_bsr_spmv(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
         y[o + 1] = r1;
         y[o + 2] = r2;
         y[o + 3] = 0;
-        red += (double)r0 * r0 + (double)r1 * r1 + (double)r2 * r2;
+        red += r0 * r0 + r1 * r1 + r2 * r2;
       }
       else {
         y[o] = y0;
@@ -238,12 +238,12 @@ k_bsr_spmv(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
         y[o + 2] = y2;
         y[o + 3] = 0;
         if(MODE == 2)
-          red += (double)p[o] * y0 + (double)p[o + 1] * y1 + (double)p[o + 2] * y2;
+          red += p[o] * y0 + p[o + 1] * y1 + p[o + 2] * y2;
       }
     }
   }
   if(MODE != 0) {
-    double s = block_sum<double, 256>(red);
+    double s = block_sum<double, 256>((double)red);
     if(threadIdx.x == 0) part[blockIdx.x] = s;
     // the consumers sum a fixed number of partials
     if(blockIdx.x == 0)
@@ -255,20 +255,6 @@ k_bsr_spmv(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
       if(threadIdx.x == 0) *dot_out = d;
     }
   }
-}
-
-// CTAs of `kernel` that fit on the device at once (at most kReduceBlocks)
-template <typename K>
-static int resident_grid(K kernel, int threads, size_t smem)
-{
-  int dev = 0, sms = 0, per_sm = 0;
-  if(cudaGetDevice(&dev) != cudaSuccess ||
-     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) !=
-       cudaSuccess ||
-     per_sm < 1 || sms < 1)
-    return kReduceBlocks;
-  return per_sm * sms < kReduceBlocks ? per_sm * sms : kReduceBlocks;
 }
 
 // ---------------------------------------------------------------------------

@@ -82,6 +82,19 @@ __device__ __forceinline__ float warp_sum(float v)
   return v;
 }
 
+// Per-thread accumulator of a reduction over vector entries of type T:
+// float for FP32 vectors (a thread sums a few dozen terms at most, FP64
+// takes over at the block sum), double otherwise.  GB300's FP64 pipe
+// retires about two FMAs (or conversions) per SM per clock, so FP64
+// arithmetic on every entry of an FP32 vector costs more time than the
+// entry's memory traffic.
+template <typename T> struct Acc {
+  using type = double;
+};
+template <> struct Acc<float> {
+  using type = float;
+};
+
 // block-wide sum in a fixed order; result valid in thread 0
 template <typename T, int NT> __device__ __forceinline__ T block_sum(T v)
 {
@@ -183,6 +196,20 @@ inline int grid_for(long long work, int threads, int max_blocks = 1 << 30)
   if(b < 1) b = 1;
   if(b > max_blocks) b = max_blocks;
   return (int)b;
+}
+
+// CTAs of `kernel` that fit on the device at once (at most kReduceBlocks):
+// a grid-stride kernel launched this wide runs in one wave
+template <typename K> int resident_grid(K kernel, int threads, size_t smem)
+{
+  int dev = 0, sms = 0, per_sm = 0;
+  if(cudaGetDevice(&dev) != cudaSuccess ||
+     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) !=
+       cudaSuccess ||
+     per_sm < 1 || sms < 1)
+    return kReduceBlocks;
+  return per_sm * sms < kReduceBlocks ? per_sm * sms : kReduceBlocks;
 }
 
 }  // namespace gb

@@ -212,13 +212,22 @@ k_cg_step(int n, CgState *__restrict__ S, T *__restrict__ x, T *__restrict__ r,
           const T *__restrict__ p, const T *__restrict__ q, double *__restrict__ part)
 {
   if(!S->go) return;
+  // alpha and the breakdown test once per CTA: FP64 divisions in every
+  // thread would keep the FP64 pipe busier than the vector traffic
+  __shared__ T s_alpha;
+  __shared__ int s_bad;
   const double pq = S->pq, rho = S->rho;
-  const int bad = cg_breakdown(pq);
-  double v = 0.;
+  if(threadIdx.x == 0) {
+    s_bad = cg_breakdown(pq);
+    s_alpha = s_bad ? (T)0 : (T)(rho / pq);
+  }
+  __syncthreads();
+  const int bad = s_bad;
+  typename Acc<T>::type v = 0;
   if(!bad) {
     // vectors are cudaMalloc'ed (256-byte aligned): groups of four, then
     // the n % 4 remainder
-    T a = (T)(rho / pq);
+    const T a = s_alpha;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long n4 = n / 4;
     for(long long i4 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i4 < n4;
@@ -232,7 +241,7 @@ k_cg_step(int n, CgState *__restrict__ S, T *__restrict__ x, T *__restrict__ r,
       for(int c = 0; c < 4; c++) {
         xv[c] += a * pv[c];
         rv[c] = rv[c] - a * qv[c];
-        v += (double)rv[c] * (double)rv[c];
+        v += rv[c] * rv[c];
       }
       st4(x, i4, xv);
       st4(r, i4, rv);
@@ -242,10 +251,10 @@ k_cg_step(int n, CgState *__restrict__ S, T *__restrict__ x, T *__restrict__ r,
       x[i] += a * p[i];
       T ri = r[i] - a * q[i];
       r[i] = ri;
-      v += (double)ri * (double)ri;
+      v += ri * ri;
     }
   }
-  double s = block_sum<double, 256>(v);
+  double s = block_sum<double, 256>((double)v);
   if(threadIdx.x == 0) part[blockIdx.x] = s;
   if(blockIdx.x == 0)
     for(int b = gridDim.x + threadIdx.x; b < kReduceBlocks; b += blockDim.x) part[b] = 0.;
@@ -309,7 +318,7 @@ k_cg_spmv(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
   const int rows_per_block = 256 / TPR;
   int lane = threadIdx.x % TPR;
   int sub = threadIdx.x / TPR;
-  double red = 0.0;
+  typename Acc<XT>::type red = 0;
   for(long long rb = (long long)blockIdx.x * rows_per_block; rb < n;
       rb += (long long)gridDim.x * rows_per_block) {
     long long row = rb + sub;
@@ -323,10 +332,10 @@ k_cg_spmv(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
       sum += __shfl_down_sync(0xffffffffu, sum, o, TPR);
     if(lane == 0 && row < n) {
       q[row] = sum;
-      red += (double)p[row] * (double)sum;
+      red += p[row] * sum;
     }
   }
-  double s = block_sum<double, 256>(red);
+  double s = block_sum<double, 256>((double)red);
   if(threadIdx.x == 0) part[blockIdx.x] = s;
   if(arrive_last(&S->tick_dot)) {
     double d = sum_partials_l2<256>(part);
@@ -376,12 +385,13 @@ static int cg_core(cudaStream_t st, int n, SPMV spmv_dot, const T *rhs, T *y,
 
   // capture a batch of iterations once
   const int batch = n > 200000 ? 16 : 32;
+  const int step_grid = resident_grid(k_cg_step<T, false>, 256, 0);
   cudaGraph_t graph;
   cudaGraphExec_t exec;
   GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   for(int it = 0; it < batch; it++) {
     spmv_dot(p, q, part, S, st);
-    k_cg_step<T, false><<<kReduceBlocks, 256, 0, st>>>(n, S, y, r, p, q, part);
+    k_cg_step<T, false><<<step_grid, 256, 0, st>>>(n, S, y, r, p, q, part);
     k_cg_p<T><<<grid_for((n + 3) / 4, 256, kReduceBlocks * 4), 256, 0, st>>>(n, S, p, r);
   }
   GB_CUDA(cudaStreamEndCapture(st, &graph));
@@ -614,12 +624,13 @@ static int cg_mixed_core(cudaStream_t st, int n, SPMV32 spmv32, RES64 res64,
   // resumes.  The iterations and their arithmetic are those of the one-graph
   // sequence; only the place where the update kernels run moves.
   const int batch = n > 200000 ? 16 : 32;
+  const int step_grid = resident_grid(k_cg_step<float, true>, 256, 0);
   cudaGraph_t graph, ugraph;
   cudaGraphExec_t exec, uexec;
   GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   for(int it = 0; it < batch; it++) {
     spmv32(p32, q32, part, S, st);
-    k_cg_step<float, true><<<kReduceBlocks, 256, 0, st>>>(n, S, x32, r32, p32, q32, part);
+    k_cg_step<float, true><<<step_grid, 256, 0, st>>>(n, S, x32, r32, p32, q32, part);
     k_cg_p<float><<<gs, 256, 0, st>>>(n, S, p32, r32);
   }
   GB_CUDA(cudaStreamEndCapture(st, &graph));

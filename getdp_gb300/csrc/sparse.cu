@@ -490,7 +490,7 @@ k_spmv(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
   const int rows_per_block = 256 / TPR;
   int lane = threadIdx.x % TPR;
   int sub = threadIdx.x / TPR;
-  double red = 0.0;
+  typename Acc<XT>::type red = 0;
   for(long long rb = (long long)blockIdx.x * rows_per_block; rb < n;
       rb += (long long)gridDim.x * rows_per_block) {
     long long row = rb + sub;
@@ -506,16 +506,16 @@ k_spmv(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
       if(MODE == 1) {
         ACC r = b[row] - sum;
         y[row] = r;
-        red += (double)r * (double)r;
+        red += r * r;
       }
       else {
         y[row] = sum;
-        if(MODE == 2) red += (double)x[row] * (double)sum;
+        if(MODE == 2) red += x[row] * sum;
       }
     }
   }
   if(MODE != 0) {
-    double s = block_sum<double, 256>(red);
+    double s = block_sum<double, 256>((double)red);
     if(threadIdx.x == 0) part[blockIdx.x] = s;
   }
 }
@@ -602,11 +602,11 @@ template <typename T>
 __global__ void k_dot_part(int n, const T *__restrict__ x,
                            const T *__restrict__ y, double *__restrict__ part)
 {
-  double v = 0.0;
+  typename Acc<T>::type v = 0;
   for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (long long)gridDim.x * blockDim.x)
-    v += (double)x[i] * (double)y[i];
-  double s = block_sum<double, 256>(v);
+    v += x[i] * y[i];
+  double s = block_sum<double, 256>((double)v);
   if(threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
