@@ -74,6 +74,9 @@ def parse():
                          "one warm-up step, then one Generate + mixed solve "
                          "capped at --profile-iterations CG iterations")
     ap.add_argument("--profile-iterations", type=int, default=64)
+    ap.add_argument("--learned-weights", default=None,
+                    help="nonlinear workload: also time the Newton loop with the learned "
+                         "correction (network weights, .npy)")
     return ap.parse_args()
 
 
@@ -554,6 +557,23 @@ def run_nonlinear(args, ws, rank, local):
         run_gpu(n, prec, 1)  # warm-up (pattern, colouring, tuning)
         res[prec], _ = run_gpu(n, prec, max(args.steps, 1))
     best = min(res.values(), key=lambda r: r["s"])
+    learned = None
+    if args.learned_weights:
+        from getdp_gb300 import learned as LR
+        net = LR.MPNN(seed=1)
+        net.set_params(np.load(args.learned_weights))
+        p = W.nonlinear_2d(n=n, seed=5)
+        dm = W.dofmap_for(p)
+        terms = G.DeviceTerms(p, dm)
+        pol = LR.NewtonSolver(net, stopping_test=1e-10, precision=1)
+        t0 = time.perf_counter()
+        r = NL.newton(terms, dm.n_dof, pol, tol_rel=1e-8, iter_max=50, relaxation=RELAX)
+        learned = {"s": time.perf_counter() - t0, "newton_steps": len(r.history) - 1,
+                   "linear_iterations": int(sum(s["iterations"] for s in r.solves)),
+                   "learned_attempt_iterations": int(sum(
+                       s.get("learned_attempt_iterations") or 0 for s in pol.log)),
+                   "solves": pol.log, "converged": r.converged,
+                   "weights": os.path.basename(args.learned_weights)}
     line = {"metric": "nonlinear 2D magnetostatics: time to 1e-8 Newton residual "
                       "(Generate + Solve per step)",
             "value": best["s"], "unit": "s", "n_gpus": ws, "steps": args.steps,
@@ -566,6 +586,8 @@ def run_nonlinear(args, ws, rank, local):
                        "elements": 2 * n * n, "unknowns": res[0]["unknowns"],
                        "parallelism": f"replicas x{ws}"},
             "fp64": res[0], "mixed": res[1]}
+    if learned is not None:
+        line["learned_mixed"] = learned
     if not args.skip_cpu and rank == 0:
         import oracle
         oracle.build()

@@ -121,6 +121,7 @@ SIGNATURES = {
     "gb300_msh_group": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_LL),
                              ctypes.POINTER(_I), ctypes.POINTER(_I), _PP, _PP, _PP]),
     "gb300_matrix_set_correction": (_I, [_P, _P, _I]),
+    "gb300_matrix_scale_correction": (_I, [_P, ctypes.c_double]),
     "gb300_precond_apply": (_I, [_P, ctypes.POINTER(SolverParams), _P, _P]),
     "gb300_mpnn_param_count": (_I, []),
     "gb300_mpnn_create": (_I, [_P, ctypes.c_uint, _PP]),

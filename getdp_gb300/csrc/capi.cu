@@ -766,6 +766,23 @@ int gb300_matrix_set_correction(gb300_matrix *A, const double *values, int on_de
   return GB300_OK;
 }
 
+int gb300_matrix_scale_correction(gb300_matrix *A, double s)
+{
+  GB_TRY(check(A, "matrix"));
+  if(!correction_valid(A)) {
+    set_error("the matrix has no correction on its current pattern");
+    return GB300_ERR_ARG;
+  }
+  cudaStream_t st = A->ctx->stream;
+  for(long long o = 0; o < A->nnz; o += (1LL << 30)) {
+    int m = (int)((A->nnz - o) < (1LL << 30) ? (A->nnz - o) : (1LL << 30));
+    k_axpby<<<grid_for(m, 256), 256, 0, st>>>(m, 0., A->corr.p + o, s, A->corr.p + o);
+  }
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(st));
+  return GB300_OK;
+}
+
 int gb300_precond_apply(gb300_matrix *A, const gb300_solver_params *p,
                         const gb300_vector *v, gb300_vector *z)
 {

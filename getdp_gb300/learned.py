@@ -5,10 +5,13 @@ width 32 over the matrix graph, BF16 weights) predicts a sparse matrix G on
 A's pattern; the preconditioner is z = ILU^-1 v, z += G (v - A z).  It is
 trained on the GPU with its own forward and backward kernels and Adam, on
 systems assembled by Generate and solutions from the plain solver: for
-each, z1 = ILU^-1 b, r1 = b - A z1, e1 = x* - z1, and the loss is
-||G r1 - e1||^2 / ||e1||^2.  solve() runs FGMRES with the correction and
-falls back to the plain ILU(0)-GMRES when that does not converge or takes
-more steps than the cap allows; the FP64 residual decides either way.
+each, z1 = ILU^-1 b, r1 = b - A z1, e1 = x* - z1, and the loss is the
+energy norm of the error left, (G r1 - e1)^T A (G r1 - e1) / e1^T A e1
+(random probes without a solution stand in with ILU^-1 r1 for e1).
+solve() scales the correction by the energy-optimal step on random probes
+(step_length), runs FGMRES with it, and falls back to the plain
+ILU(0)-GMRES when the step is too small, or when FGMRES does not converge
+within the cap; the FP64 residual decides either way.
 """
 from __future__ import annotations
 
@@ -123,6 +126,53 @@ def make_probes(A: LA.gMatrix, count: int, seed: int, renumbering: int = 1) -> l
     return out
 
 
+def copy_matrix(A: LA.gMatrix) -> LA.gMatrix:
+    """A new matrix with A's CSR (through the host): training keeps the
+    Jacobians of every Newton step while the solver reuses A."""
+    ip, ix, dv = A.csr()
+    B = LA.gMatrix(A.n)
+    B.set_csr(ip, ix, dv)
+    return B
+
+
+def copy_vector(v: LA.gVector) -> LA.gVector:
+    w = LA.gVector(v.n)
+    v._flush()
+    check(_lib.load().gb300_vector_axpby(1.0, v.h, 0.0, w.h))
+    return w
+
+
+def step_length(A: LA.gMatrix, probes: int = 2, seed: int = 0, renumbering: int = 1,
+                precision: int = 0) -> float:
+    """The step along the attached correction that minimises the energy norm
+    of the error left after the ILU step, averaged over random probes v:
+    with z1 = ILU^-1 v, r1 = v - A z1 and g = G r1, the error after
+    z1 + w g is smallest in the A-norm at w = r1.g / g.Ag (A symmetric
+    positive definite).  A value <= 0 means the correction does not help."""
+    L = _lib.load()
+    rng = np.random.default_rng(seed)
+    n = A.n
+    S6 = ilu_params(renumbering)
+    S6.set("Precision", precision)
+    S20 = ilu_params(renumbering)
+    S20.set("Preconditioner", 20)
+    S20.set("Precision", precision)
+    v, z1, z2, r1, ag = (LA.gVector(n) for _ in range(5))
+    num = den = 0.0
+    for _ in range(probes):
+        v.set(rng.standard_normal(n))
+        check(L.gb300_precond_apply(A.h, ctypes.byref(S6.params), v.h, z1.h))
+        check(L.gb300_precond_apply(A.h, ctypes.byref(S20.params), v.h, z2.h))
+        check(L.gb300_vector_axpby(-1.0, z1.h, 1.0, z2.h))    # g = z2 - z1
+        check(L.gb300_matrix_mult(A.h, z1.h, r1.h))
+        check(L.gb300_vector_axpby(1.0, v.h, -1.0, r1.h))     # r1 = v - A z1
+        check(L.gb300_matrix_mult(A.h, z2.h, ag.h))           # A g
+        g, r, a = z2.numpy(), r1.numpy(), ag.numpy()
+        num += float(r @ g)
+        den += float(g @ a)
+    return num / den if den > 0 else 0.0
+
+
 def train(net: MPNN, samples: list, epochs: int = 20, lr: float = 3e-3,
           batch: int = 8, seed: int = 0) -> list:
     """Adam on mini-batches of systems; returns the mean loss per epoch."""
@@ -144,10 +194,21 @@ def train(net: MPNN, samples: list, epochs: int = 20, lr: float = 3e-3,
 
 def solve(A: LA.gMatrix, b: LA.gVector, x: LA.gVector, net: MPNN,
           stopping_test: float = 1e-8, krylov: int = 50, nb_iter_max: int = 20000,
-          renumbering: int = 1, precision: int = 0, cap: int = None) -> dict:
+          renumbering: int = 1, precision: int = 0, cap: int = None,
+          line_search: bool = True, min_step: float = 0.05) -> dict:
     """FGMRES with the learned correction; the plain ILU(0)-GMRES if that
-    stagnates (no convergence within `cap` steps)."""
+    stagnates (no convergence within `cap` steps).  With line_search the
+    correction is first scaled by step_length(A), and not used at all when
+    that step is below min_step."""
     net.infer(A)
+    omega = None
+    if line_search:
+        omega = step_length(A, renumbering=renumbering, precision=precision)
+        if omega < min_step:
+            return _plain(A, b, x, stopping_test, krylov, nb_iter_max, renumbering,
+                          precision, dict(learned_attempt_iterations=0, step=omega,
+                                          preconditioner="ilu0 (correction rejected)"))
+        check(_lib.load().gb300_matrix_scale_correction(A.h, ctypes.c_double(omega)))
     S = LA.LinAlg_CreateSolver(None)
     for k, v in dict(Algorithm=9, Preconditioner=20, Krylov_Size=krylov,
                      Nb_Iter_Max=cap or nb_iter_max, Renumbering_Technique=renumbering,
@@ -156,15 +217,60 @@ def solve(A: LA.gMatrix, b: LA.gVector, x: LA.gVector, net: MPNN,
     S["stopping_test"] = stopping_test
     info = LA.LinAlg_Solve(A, b, S, x)
     info["preconditioner"] = "learned"
+    info["step"] = omega
     if info["status"] == 0:
         return info
+    return _plain(A, b, x, stopping_test, krylov, nb_iter_max, renumbering, precision,
+                  dict(learned_attempt_iterations=info["iterations"], step=omega,
+                       preconditioner="ilu0 (fallback)"))
+
+
+def _plain(A, b, x, stopping_test, krylov, nb_iter_max, renumbering, precision, extra):
+    """The method without the network: ILU(0)-GMRES, or FGMRES with the
+    FP32 factor (Precision 1)."""
     P = LA.LinAlg_CreateSolver(None)
-    for k, v in dict(Algorithm=8, Preconditioner=6, Krylov_Size=krylov,
-                     Nb_Iter_Max=nb_iter_max, Renumbering_Technique=renumbering,
-                     Precision=precision).items():
+    for k, v in dict(Algorithm=8 if precision == 0 else 9, Preconditioner=6,
+                     Krylov_Size=krylov, Nb_Iter_Max=nb_iter_max,
+                     Renumbering_Technique=renumbering, Precision=precision).items():
         P.set(k, v)
     P["stopping_test"] = stopping_test
     plain = LA.LinAlg_Solve(A, b, P, x)
-    plain["preconditioner"] = "ilu0 (fallback)"
-    plain["learned_attempt_iterations"] = info["iterations"]
+    plain.update(extra)
     return plain
+
+
+class NewtonSolver:
+    """The linear solve of each Newton step with the learned correction, as
+    a callable for nonlinear.newton: the learned FGMRES is capped at the
+    step count of the last plain solve (iterations not reduced = fallback),
+    the first attempt at `first_cap`; after `max_failures` failed attempts
+    the remaining steps use the plain method directly."""
+
+    def __init__(self, net: MPNN, stopping_test: float = 1e-10, krylov: int = 50,
+                 nb_iter_max: int = 20000, renumbering: int = 1, precision: int = 1,
+                 first_cap: int = 2000, max_failures: int = 1):
+        self.net = net
+        self.kw = dict(stopping_test=stopping_test, krylov=krylov,
+                       nb_iter_max=nb_iter_max, renumbering=renumbering,
+                       precision=precision)
+        self.first_cap = first_cap
+        self.max_failures = max_failures
+        self.failures = 0
+        self.last_plain = None
+        self.log = []
+
+    def __call__(self, A: LA.gMatrix, b: LA.gVector, x: LA.gVector) -> dict:
+        if self.failures >= self.max_failures:
+            info = _plain(A, b, x, self.kw["stopping_test"], self.kw["krylov"],
+                          self.kw["nb_iter_max"], self.kw["renumbering"],
+                          self.kw["precision"], dict(preconditioner="ilu0 (learned off)"))
+        else:
+            cap = self.last_plain if self.last_plain else self.first_cap
+            info = solve(A, b, x, self.net, cap=cap, **self.kw)
+            if info["preconditioner"] != "learned":
+                self.failures += 1
+        if info["preconditioner"] != "learned":
+            self.last_plain = info["iterations"]
+        self.log.append({k: info.get(k) for k in ("preconditioner", "iterations",
+                                                  "learned_attempt_iterations", "step")})
+        return info

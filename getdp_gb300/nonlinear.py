@@ -33,13 +33,16 @@ class NewtonResult:
     converged: bool
 
 
-def newton(terms: G.DeviceTerms, n: int, solver: LA.gSolver, tol_rel: float = 1e-8,
+def newton(terms: G.DeviceTerms, n: int, solver, tol_rel: float = 1e-8,
            tol_abs: float = 1e-300, iter_max: int = 50, A: LA.gMatrix = None,
            b: LA.gVector = None, relaxation=(1.0,)) -> NewtonResult:
     """With several relaxation factors the step dx of each Solve is relaxed
     as SolveJac_AdaptRelax does with CheckAll 0 (SolvingOperations.cpp:
     1593-1700): the factors are tried in order, x + f dx regenerated and its
-    residual ||b - A x|| / N kept while it decreases; the best is taken."""
+    residual ||b - A x|| / N kept while it decreases; the best is taken.
+    `solver` is a gSolver for LinAlg_Solve, or a callable (A, b, x) -> info
+    dict that solves A x = b in its place (the learned preconditioner's
+    solve, for one)."""
     A = A if A is not None else LA.gMatrix(n)
     b = b if b is not None else LA.gVector(n)
     x = LA.gVector(n)  # InitSolution: zero
@@ -54,13 +57,18 @@ def newton(terms: G.DeviceTerms, n: int, solver: LA.gSolver, tol_rel: float = 1e
         G.generate(A, b, terms.batch, pattern=first[0], solution=x)
         first[0] = False
 
+    def linear(x_):
+        if callable(solver):
+            return solver(A, b, x_)
+        return LA.LinAlg_Solve(A, b, solver, x_)
+
     def solve():
         if x_save is None:
-            solves.append(LA.LinAlg_Solve(A, b, solver, x))
+            solves.append(linear(x))
             generate()
             return
         _lib.check(L.gb300_vector_axpby(1.0, x.h, 0.0, x_save.h))
-        solves.append(LA.LinAlg_Solve(A, b, solver, x))
+        solves.append(linear(x))
         _lib.check(L.gb300_vector_axpby(1.0, x.h, 0.0, dx.h))
         _lib.check(L.gb300_vector_axpby(-1.0, x_save.h, 1.0, dx.h))  # dx = x_new - x
         err_prev, f_opt = 1e99, relaxation[0]

@@ -297,6 +297,8 @@ int gb300_residual_noalloc(gb300_matrix *A, const gb300_vector *x,
    matrix on A's pattern.  gb300_matrix_set_correction attaches G (values in
    A's CSR order, host or device pointer); a pattern change drops it. */
 int gb300_matrix_set_correction(gb300_matrix *A, const double *values, int on_device);
+/* G <- s G for the attached correction (a per-system step length) */
+int gb300_matrix_scale_correction(gb300_matrix *A, double s);
 /* z = M^-1 v with the preconditioner the solver would use for p
    (Preconditioner 6 or 20; Renumbering_Technique selects the ordering) on
    A's unscaled values. */
