@@ -421,6 +421,9 @@ struct GmState {
   double H[(kMaxKrylov + 1) * kMaxKrylov];  // column-major, (m+1) x m
   double cs[kMaxKrylov], sn[kMaxKrylov], g[kMaxKrylov + 1], y[kMaxKrylov];
   double h1[kMaxKrylov + 1], h2[kMaxKrylov + 1];
+  double nrm0;      // ||w||^2 before the Gram-Schmidt pass of this step
+  int reorth;       // this step takes a second Gram-Schmidt pass
+  int reorths;      // second passes taken so far
 };
 
 // restart: r = rhs - A x was computed with its partial norms
@@ -465,14 +468,19 @@ __global__ void k_gm_scale(int n, const GmState *__restrict__ S,
     y[i] = s * x[i];
 }
 
-// partial dots <V_j, w>, j < k, over a fixed grid; part[j * B + block]
+// partial dots <V_j, w>, j < k, over a fixed grid; part[j * B + block].
+// PASS 0 also forms <w, w> (as column k), the norm the selective
+// re-orthogonalisation compares with; PASS 1 runs only when this step
+// takes the second Gram-Schmidt pass.
+template <int PASS>
 __global__ void __launch_bounds__(256)
 k_gm_dots(int n, int k, const double *__restrict__ V, size_t ldv,
           const double *__restrict__ w, double *__restrict__ part,
           const GmState *__restrict__ S)
 {
-  if(!S->cycle) return;
-  for(int j0 = 0; j0 < k; j0 += 8) {
+  if(!S->cycle || (PASS == 1 && !S->reorth)) return;
+  const int kk = PASS == 0 ? k + 1 : k;  // column k: V_k = w itself
+  for(int j0 = 0; j0 < kk; j0 += 8) {
     double acc[8];
 #pragma unroll
     for(int u = 0; u < 8; u++) acc[u] = 0.;
@@ -481,36 +489,60 @@ k_gm_dots(int n, int k, const double *__restrict__ V, size_t ldv,
       double wi = w[i];
 #pragma unroll
       for(int u = 0; u < 8; u++)
-        if(j0 + u < k) acc[u] += V[(size_t)(j0 + u) * ldv + i] * wi;
+        if(j0 + u < kk) acc[u] += V[(size_t)(j0 + u) * ldv + i] * wi;
     }
 #pragma unroll
     for(int u = 0; u < 8; u++) {
-      if(j0 + u >= k) break;
+      if(j0 + u >= kk) break;
       double s = block_sum<double, 256>(acc[u]);
       if(threadIdx.x == 0) part[(size_t)(j0 + u) * kReduceBlocks + blockIdx.x] = s;
     }
   }
 }
 
-// h[j] = sum of partials (one warp per j); pass 0 stores, pass 1 adds
+// h[j] = sum of partials (one warp per j); pass 0 stores h1 (and the
+// column of H) and ||w||^2, pass 1 stores h2 and adds it to the column
 __global__ void k_gm_reduce(int k, const double *__restrict__ part, GmState *S,
                             int pass, int nb)
 {
-  if(!S->cycle) return;
+  if(!S->cycle || (pass == 1 && !S->reorth)) return;
   int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for(int j = w; j < k; j += blockDim.x / 32) {
+  const int kk = pass == 0 ? k + 1 : k;
+  for(int j = w; j < kk; j += blockDim.x / 32) {
     double v = 0.;
     for(int b = lane; b < nb; b += 32) v += part[(size_t)j * kReduceBlocks + b];
     v = warp_sum(v);
     if(lane == 0) {
-      if(pass == 0)
+      if(j == k)
+        S->nrm0 = v;
+      else if(pass == 0) {
         S->h1[j] = v;
+        S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = v;
+      }
       else {
         S->h2[j] = v;
         S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = S->h1[j] + v;
       }
     }
   }
+}
+
+// Selective re-orthogonalisation with mgsro's constant (iters.f:3475-3600,
+// reorth = 0.98): mgsro repeats the projection on one basis vector when it
+// removed more than 98 % of the squared norm left; here the second
+// classical Gram-Schmidt pass runs when the first pass removed more than
+// 98 % of ||w||^2 (||w'|| < 0.14 ||w||).  The loss of orthogonality of one
+// pass grows like eps ||w|| / ||w'||, so a pass that keeps more than 2 % of
+// ||w||^2 leaves w' orthogonal to within ~10 eps.
+__global__ void k_gm_reorth_test(GmState *S, const double *__restrict__ pn, int nb)
+{
+  if(!S->cycle) return;
+  double rr = 0.;
+  for(int i = threadIdx.x; i < nb; i += blockDim.x) rr += pn[i];
+  rr = block_sum<double, 256>(rr);
+  if(threadIdx.x) return;
+  S->reorth = !(rr >= 0.02 * S->nrm0);
+  if(S->reorth) S->reorths += 1;
 }
 
 // w -= sum_j h_j V_j (h from pass `pass`); with NORM the partial ||w||^2
@@ -520,7 +552,7 @@ k_gm_update(int n, int k, const double *__restrict__ V, size_t ldv,
             double *__restrict__ w, double *__restrict__ part,
             const GmState *__restrict__ S, int pass)
 {
-  if(!S->cycle) return;
+  if(!S->cycle || (pass == 1 && !S->reorth)) return;
   __shared__ double h[kMaxKrylov];
   for(int j = threadIdx.x; j < k; j += blockDim.x)
     h[j] = pass == 0 ? S->h1[j] : S->h2[j];
@@ -756,11 +788,12 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   double *zt = (double *)W.vec(4, sizeof(double) * n);
   float *t32 = fp32 ? (float *)W.vec(5, sizeof(float) * n) : nullptr;
   double *part = (double *)W.vec(6, sizeof(double) * kReduceBlocks * (m + 1));
+  double *pn = (double *)W.vec(12, sizeof(double) * kReduceBlocks);
   GmState *S = (GmState *)W.state(sizeof(GmState));
   int *okflag = (int *)W.vec(7, sizeof(int));
   double *t1 = learned ? (double *)W.vec(8, sizeof(double) * n) : nullptr;
   double *t2 = learned ? (double *)W.vec(9, sizeof(double) * n) : nullptr;
-  if(!V || (flexible && !Z) || !r || !u || !zt || (fp32 && !t32) || !part || !S ||
+  if(!V || (flexible && !Z) || !r || !u || !zt || (fp32 && !t32) || !part || !pn || !S ||
      (learned && (!t1 || !t2)))
     return GB300_ERR_CUDA;
   GmState h0;
@@ -799,13 +832,16 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
     double *z = flexible ? Z + (size_t)(k - 1) * ldv : zt;
     precond_apply(vk, z, cycle_flag(S));
     spmv_guarded(A, val, z, w, &S->cycle, st);
-    k_gm_dots<<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S);
+    // classical Gram-Schmidt, a second pass only when the test asks for
+    // it; both passes leave the partials of ||w||^2 in pn
+    k_gm_dots<0><<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S);
     k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 0, nb);
-    k_gm_update<0><<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S, 0);
-    k_gm_dots<<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S);
+    k_gm_update<1><<<nb, 256, 0, st>>>(n, k, V, ldv, w, pn, S, 0);
+    k_gm_reorth_test<<<1, 256, 0, st>>>(S, pn, nb);
+    k_gm_dots<1><<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S);
     k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 1, nb);
-    k_gm_update<1><<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S, 1);
-    k_gm_step<<<1, 256, 0, st>>>(k, m, S, part, nb);
+    k_gm_update<1><<<nb, 256, 0, st>>>(n, k, V, ldv, w, pn, S, 1);
+    k_gm_step<<<1, 256, 0, st>>>(k, m, S, pn, nb);
     k_gm_scale_next<<<gs, 256, 0, st>>>(n, S, w, k);
   }
   k_gm_solve_small<<<1, 32, 0, st>>>(S);

@@ -349,6 +349,7 @@ static void cg_spmv(const gb300_matrix *A, const V *val, const XT *p, XT *q,
 {
   int n = A->n;
   switch(A->tpr) {
+  case 2: k_cg_spmv<2><<<kReduceBlocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, p, q, part, S); break;
   case 4: k_cg_spmv<4><<<kReduceBlocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, p, q, part, S); break;
   case 8: k_cg_spmv<8><<<kReduceBlocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, p, q, part, S); break;
   case 16: k_cg_spmv<16><<<kReduceBlocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, p, q, part, S); break;

@@ -144,6 +144,7 @@ extern "C" int gb300_residual_noalloc(gb300_matrix *A, const gb300_vector *x,
   int nb = n > 0 ? (int)((n + kRowsPerBlock - 1) / kRowsPerBlock) : 0;
   if(nb > 0) {
     switch(A->tpr) {
+    case 2: k_residual_noalloc<2><<<nb, kNoAllocThreads, 0, st>>>(n, A->rowptr.p, A->col.p, A->val.p, x->d.p, b->d.p, r->d.p, scratch); break;
     case 4: k_residual_noalloc<4><<<nb, kNoAllocThreads, 0, st>>>(n, A->rowptr.p, A->col.p, A->val.p, x->d.p, b->d.p, r->d.p, scratch); break;
     case 8: k_residual_noalloc<8><<<nb, kNoAllocThreads, 0, st>>>(n, A->rowptr.p, A->col.p, A->val.p, x->d.p, b->d.p, r->d.p, scratch); break;
     case 16: k_residual_noalloc<16><<<nb, kNoAllocThreads, 0, st>>>(n, A->rowptr.p, A->col.p, A->val.p, x->d.p, b->d.p, r->d.p, scratch); break;

@@ -469,7 +469,10 @@ int build_csr_from_coo(gb300_matrix *A, long long m, const int *d_r,
 void choose_tpr(gb300_matrix *A)
 {
   double avg = A->n ? (double)A->nnz / A->n : 0.0;
-  A->tpr = avg > 24 ? 32 : avg > 12 ? 16 : avg > 6 ? 8 : 4;
+  // few lanes per row: GB300's FP64 pipe (about two FMAs per SM per clock)
+  // makes the lanes left idle on a short row, and the shuffle-add tree of
+  // the row sum, cost more than the row's memory traffic
+  A->tpr = avg > 128 ? 32 : avg > 64 ? 16 : avg > 32 ? 8 : avg > 16 ? 4 : 2;
 }
 
 // ---------------------------------------------------------------------------
@@ -531,6 +534,9 @@ static void launch_spmv(const gb300_matrix *A, const V *val, const XT *x,
                            : kReduceBlocks;
   if(MODE == 0 && blocks > 152 * 64) blocks = 152 * 64;
   switch(A->tpr) {
+  case 2:
+    k_spmv<2, MODE><<<blocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, x, b, y, part, flag);
+    break;
   case 4:
     k_spmv<4, MODE><<<blocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, x, b, y, part, flag);
     break;
