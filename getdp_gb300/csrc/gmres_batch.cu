@@ -10,7 +10,8 @@
 // keeps its own Krylov state (Hessenberg matrix, Givens rotations,
 // residual, counters, flags), so its iterations are those of the
 // single-system solver of gmres.cu (iters.f:1912-2219 for GMRES,
-// :2522-2806 for FGMRES, with CGS2 orthogonalisation): it converges, stops
+// :2522-2806 for FGMRES, with classical Gram-Schmidt and the selective
+// second pass of gmres.cu): it converges, stops
 // at its own iteration cap or breaks down on its own; the chunks of a
 // system that has stopped are skipped.  All systems run their restart
 // cycles in step (a cycle ends early only for a system that has
@@ -27,7 +28,9 @@ constexpr int kBMaxKrylov = 128;
 
 struct BState {
   double rtol, tol, res, res0, res6, scale;
+  double nrm0;  // ||w||^2 before this step's Gram-Schmidt pass
   int its, maxit, status, active, cycle, first, k, did_cycle, breakdown;
+  int reorth;   // this step takes the second Gram-Schmidt pass
 };
 
 // per-system Krylov arrays, m = restart length
@@ -172,14 +175,19 @@ __global__ void k_b_scale(Chunks C, BView V, const double *x, double *y, int K)
   }
 }
 
-// partial dots <V_j, w>, j < k, per chunk: part[j * nchunks + c]
+// partial dots <V_j, w>, j < k, per chunk: part[j * nchunks + c]; PASS 0
+// also <w, w> (column k: V_k is w), PASS 1 only for systems whose step
+// takes the second pass
+template <int PASS>
 __global__ void __launch_bounds__(kBThreads)
 k_b_dots(Chunks C, int k, const double *__restrict__ Vb, size_t ldv,
          const double *__restrict__ w, double *__restrict__ part, BView V)
 {
+  const int kk = PASS == 0 ? k + 1 : k;
   for(int c = blockIdx.x; c < C.n; c += gridDim.x) {
-    if(!V.S[C.sys[c]].cycle) continue;
-    for(int j0 = 0; j0 < k; j0 += 8) {
+    const BState &s = V.S[C.sys[c]];
+    if(!s.cycle || (PASS == 1 && !s.reorth)) continue;
+    for(int j0 = 0; j0 < kk; j0 += 8) {
       double acc[8];
 #pragma unroll
       for(int u = 0; u < 8; u++) acc[u] = 0.;
@@ -187,11 +195,11 @@ k_b_dots(Chunks C, int k, const double *__restrict__ Vb, size_t ldv,
         double wi = w[i];
 #pragma unroll
         for(int u = 0; u < 8; u++)
-          if(j0 + u < k) acc[u] += Vb[(size_t)(j0 + u) * ldv + i] * wi;
+          if(j0 + u < kk) acc[u] += Vb[(size_t)(j0 + u) * ldv + i] * wi;
       }
 #pragma unroll
       for(int u = 0; u < 8; u++) {
-        if(j0 + u >= k) break;
+        if(j0 + u >= kk) break;
         double s = block_sum<double, kBThreads>(acc[u]);
         if(threadIdx.x == 0) part[(size_t)(j0 + u) * C.n + c] = s;
       }
@@ -205,13 +213,18 @@ __global__ void k_b_reduce(int nsys, int k, Chunks C, const double *__restrict__
 {
   int p = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   int lane = threadIdx.x & 31;
-  if(p >= nsys || !V.S[p].cycle) return;
-  for(int j = lane; j < k; j += 32) {
+  if(p >= nsys || !V.S[p].cycle || (pass == 1 && !V.S[p].reorth)) return;
+  const int kk = pass == 0 ? k + 1 : k;
+  for(int j = lane; j < kk; j += 32) {
     double v = 0.;
     for(int c = C.cb[p]; c < C.cb[p + 1]; c++) v += part[(size_t)j * C.n + c];
     size_t o = (size_t)p * V.m + j;
-    if(pass == 0)
+    if(j == k)
+      V.S[p].nrm0 = v;
+    else if(pass == 0) {
       V.h1[o] = v;
+      V.Hcol(p, k - 1)[j] = v;
+    }
     else {
       V.h2[o] = v;
       V.Hcol(p, k - 1)[j] = V.h1[o] + v;
@@ -228,7 +241,7 @@ k_b_update(Chunks C, int k, const double *__restrict__ Vb, size_t ldv,
   __shared__ double h[kBMaxKrylov];
   for(int c = blockIdx.x; c < C.n; c += gridDim.x) {
     int p = C.sys[c];
-    if(!V.S[p].cycle) continue;
+    if(!V.S[p].cycle || (pass == 1 && !V.S[p].reorth)) continue;
     const double *hs = (pass == 0 ? V.h1 : V.h2) + (size_t)p * V.m;
     __syncthreads();  // the previous chunk is done with h
     for(int j = threadIdx.x; j < k; j += blockDim.x) h[j] = hs[j];
@@ -245,6 +258,20 @@ k_b_update(Chunks C, int k, const double *__restrict__ Vb, size_t ldv,
       if(threadIdx.x == 0) part[c] = s;
     }
   }
+}
+
+// the selective re-orthogonalisation test of gmres.cu per system: a second
+// pass when the first removed more than 98 % of ||w||^2
+__global__ void k_b_reorth_test(int nsys, Chunks C, const double *__restrict__ pn,
+                                BView V)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if(p >= nsys) return;
+  BState &S = V.S[p];
+  if(!S.cycle) return;
+  double rr = 0.;
+  for(int c = C.cb[p]; c < C.cb[p + 1]; c++) rr += pn[c];
+  S.reorth = !(rr >= 0.02 * S.nrm0);
 }
 
 // end of an Arnoldi step per system: h(k+1,k), rotations, stopping test
@@ -519,7 +546,9 @@ int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
   float *t32 = fp32 ? (float *)W.vec(5, sizeof(float) * n) : nullptr;
   double *part = (double *)W.vec(6, sizeof(double) * (size_t)(nch > 0 ? nch : 1) * (m + 1));
   double *part2 = (double *)W.vec(7, sizeof(double) * (nch > 0 ? nch : 1));
-  if(!Vb || (flexible && !Z) || !r || !u || !zt || (fp32 && !t32) || !part || !part2)
+  double *pn = (double *)W.vec(12, sizeof(double) * (nch > 0 ? nch : 1));
+  if(!Vb || (flexible && !Z) || !r || !u || !zt || (fp32 && !t32) || !part || !part2 ||
+     !pn)
     return GB300_ERR_CUDA;
   GB_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
 
@@ -541,7 +570,7 @@ int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
   cudaGraph_t graph;
   cudaGraphExec_t exec;
   GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  k_b_residual<4, 0><<<gchunks, kBThreads, 0, st>>>(C, A->rowptr.p, A->col.p, val, x,
+  k_b_residual<2, 0><<<gchunks, kBThreads, 0, st>>>(C, A->rowptr.p, A->col.p, val, x,
                                                     rhs, r, part, nullptr, V);
   k_b_restart<<<gsys, 128, 0, st>>>(nsys, V, dcb.p, part);
   k_b_flags<<<1, 256, 0, st>>>(nsys, V, flags.p);
@@ -551,14 +580,15 @@ int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
     double *w = Vb + (size_t)k * ldv;
     double *z = flexible ? Z + (size_t)(k - 1) * ldv : zt;
     precond_apply(vk, z, flags.p, 0);
-    k_b_spmv<4><<<gchunks, kBThreads, 0, st>>>(C, A->rowptr.p, A->col.p, val, z, w, V);
-    k_b_dots<<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, part, V);
+    k_b_spmv<2><<<gchunks, kBThreads, 0, st>>>(C, A->rowptr.p, A->col.p, val, z, w, V);
+    k_b_dots<0><<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, part, V);
     k_b_reduce<<<gwarp, 256, 0, st>>>(nsys, k, C, part, V, 0);
-    k_b_update<0><<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, part, V, 0);
-    k_b_dots<<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, part, V);
+    k_b_update<1><<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, pn, V, 0);
+    k_b_reorth_test<<<gsys, 128, 0, st>>>(nsys, C, pn, V);
+    k_b_dots<1><<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, part, V);
     k_b_reduce<<<gwarp, 256, 0, st>>>(nsys, k, C, part, V, 1);
-    k_b_update<1><<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, part, V, 1);
-    k_b_step<<<gsys, 128, 0, st>>>(nsys, k, C, part, V);
+    k_b_update<1><<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, pn, V, 1);
+    k_b_step<<<gsys, 128, 0, st>>>(nsys, k, C, pn, V);
     k_b_flags<<<1, 256, 0, st>>>(nsys, V, flags.p);
     k_b_scale<<<gchunks, kBThreads, 0, st>>>(C, V, w, w, k);
   }
@@ -601,7 +631,7 @@ int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
   }
 
   // per-system results and true residuals
-  k_b_residual<4, 1><<<gchunks, kBThreads, 0, st>>>(C, A->rowptr.p, A->col.p, val, x,
+  k_b_residual<2, 1><<<gchunks, kBThreads, 0, st>>>(C, A->rowptr.p, A->col.p, val, x,
                                                     rhs, r, part, part2, V);
   GB_CUDA(cudaGetLastError());
   std::vector<BState> hsys(nsys);
