@@ -130,3 +130,41 @@ def test_gpu_training_lowers_held_out_loss_and_solve_falls_back_safely():
     # a cap of one step forces the fallback
     info = LR.solve(A, b, xs, net, stopping_test=1e-12, cap=1)
     assert info["preconditioner"].startswith("ilu0") and info["status"] == 0
+
+
+@pytest.mark.gpu
+def test_gpu_step_length_and_newton_policy():
+    """The energy-optimal step along a correction is 1 for G = A^-1 on the
+    ILU residual's span (here: a scaled exact correction is rescaled back),
+    and the Newton policy switches the correction off after a failed
+    attempt while the loop still converges."""
+    G, LR, LA = _gpu()
+    import ctypes
+    from getdp_gb300 import _lib
+    from getdp_gb300 import nonlinear as NL
+    p = W.nonlinear_2d(n=16, seed=3)
+    dm = W.dofmap_for(p)
+    A, b = G.generate_problem(p, dm)
+    net = LR.MPNN(seed=2)
+    # an untrained head predicts G = 0: no step can be taken along it
+    net.infer(A)
+    assert LR.step_length(A) == 0.0
+    # scaling a correction scales the step inversely
+    A.assemble()
+    rng = np.random.default_rng(0)
+    vals = rng.standard_normal(A.nnz()) * 1e-3
+    L = _lib.load()
+    _lib.check(L.gb300_matrix_set_correction(A.h, vals.ctypes.data_as(ctypes.c_void_p), 0))
+    s1 = LR.step_length(A)
+    _lib.check(L.gb300_matrix_scale_correction(A.h, ctypes.c_double(2.0)))
+    s2 = LR.step_length(A)
+    assert s1 != 0.0 and abs(s2 * 2.0 - s1) <= 1e-9 * abs(s1), (s1, s2)
+    # policy: a cap of one step makes the first attempt fail, then it is off
+    terms = G.DeviceTerms(p, dm)
+    pol = LR.NewtonSolver(net, stopping_test=1e-10, precision=1, first_cap=1)
+    r = NL.newton(terms, dm.n_dof, pol, tol_rel=1e-8, iter_max=50,
+                  relaxation=(1.0, 0.5, 0.25, 0.125))
+    assert r.converged
+    kinds = [s["preconditioner"] for s in pol.log]
+    assert kinds[0] != "learned"
+    assert all(k == "ilu0 (learned off)" for k in kinds[1:]), kinds
