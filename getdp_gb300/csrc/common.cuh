@@ -109,6 +109,50 @@ template <typename T, int NT> __device__ __forceinline__ T block_sum(T v)
   return s;
 }
 
+// Block-wide sums of eight per-thread accumulators, in a fixed order.
+// Within a warp a transposing butterfly halves the accumulators a lane
+// carries at each of the first three exchanges (offsets 16, 8, 4) and then
+// adds across the remaining lane pairs: 9 FP64 additions per lane instead
+// of 8 x 5 for eight separate warp sums (GB300's FP64 pipe makes the
+// difference visible).  Afterwards lane l of each warp holds the warp total
+// of accumulator (l >> 2) & 7.  out[j] is valid in thread j (j < 8).
+template <int NT> __device__ __forceinline__ double block_sum8(const double (&a)[8])
+{
+  __shared__ double red[NT / 32][8];
+  const int lane = threadIdx.x & 31;
+  double b[4], c[2], d;
+  {
+    const bool hi = lane & 16;
+#pragma unroll
+    for(int m = 0; m < 4; m++) {
+      double keep = hi ? a[m + 4] : a[m], send = hi ? a[m] : a[m + 4];
+      b[m] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+  }
+  {
+    const bool hi = lane & 8;
+#pragma unroll
+    for(int m = 0; m < 2; m++) {
+      double keep = hi ? b[m + 2] : b[m], send = hi ? b[m] : b[m + 2];
+      c[m] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+  }
+  {
+    const bool hi = lane & 4;
+    double keep = hi ? c[1] : c[0], send = hi ? c[0] : c[1];
+    d = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  d += __shfl_xor_sync(0xffffffffu, d, 2);
+  d += __shfl_xor_sync(0xffffffffu, d, 1);
+  if((lane & 3) == 0) red[threadIdx.x >> 5][lane >> 2] = d;
+  __syncthreads();
+  double s = 0.;
+  if(threadIdx.x < 8)
+    for(int w = 0; w < NT / 32; w++) s += red[w][threadIdx.x];
+  __syncthreads();
+  return s;
+}
+
 // Completion of a grid-wide reduction inside the kernel that produces the
 // partials: every block calls arrive_last after its partials are stored;
 // exactly one block, the last to arrive, gets true and then sees every

@@ -491,12 +491,9 @@ k_gm_dots(int n, int k, const double *__restrict__ V, size_t ldv,
       for(int u = 0; u < 8; u++)
         if(j0 + u < kk) acc[u] += V[(size_t)(j0 + u) * ldv + i] * wi;
     }
-#pragma unroll
-    for(int u = 0; u < 8; u++) {
-      if(j0 + u >= kk) break;
-      double s = block_sum<double, 256>(acc[u]);
-      if(threadIdx.x == 0) part[(size_t)(j0 + u) * kReduceBlocks + blockIdx.x] = s;
-    }
+    double s = block_sum8<256>(acc);
+    if(threadIdx.x < 8 && j0 + (int)threadIdx.x < kk)
+      part[(size_t)(j0 + threadIdx.x) * kReduceBlocks + blockIdx.x] = s;
   }
 }
 

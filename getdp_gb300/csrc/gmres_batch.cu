@@ -197,12 +197,9 @@ k_b_dots(Chunks C, int k, const double *__restrict__ Vb, size_t ldv,
         for(int u = 0; u < 8; u++)
           if(j0 + u < kk) acc[u] += Vb[(size_t)(j0 + u) * ldv + i] * wi;
       }
-#pragma unroll
-      for(int u = 0; u < 8; u++) {
-        if(j0 + u >= kk) break;
-        double s = block_sum<double, kBThreads>(acc[u]);
-        if(threadIdx.x == 0) part[(size_t)(j0 + u) * C.n + c] = s;
-      }
+      double s = block_sum8<kBThreads>(acc);
+      if(threadIdx.x < 8 && j0 + (int)threadIdx.x < kk)
+        part[(size_t)(j0 + threadIdx.x) * C.n + c] = s;
     }
   }
 }
