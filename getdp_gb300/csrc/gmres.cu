@@ -472,6 +472,27 @@ __global__ void k_gm_scale(int n, const GmState *__restrict__ S,
 // PASS 0 also forms <w, w> (as column k), the norm the selective
 // re-orthogonalisation compares with; PASS 1 runs only when this step
 // takes the second Gram-Schmidt pass.
+// the partial dots of columns [j0, j0 + CNT) over this CTA's share of rows
+template <int CNT>
+__device__ __forceinline__ void dots_group(int n, int j0, const double *__restrict__ V,
+                                           size_t ldv, const double *__restrict__ w,
+                                           double *__restrict__ part)
+{
+  double acc[8];
+#pragma unroll
+  for(int u = 0; u < 8; u++) acc[u] = 0.;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x) {
+    double wi = w[i];
+#pragma unroll
+    for(int u = 0; u < CNT; u++) acc[u] += V[(size_t)(j0 + u) * ldv + i] * wi;
+  }
+  double s = block_sum8<256>(acc);
+  if(threadIdx.x < CNT) part[(size_t)(j0 + threadIdx.x) * kReduceBlocks + blockIdx.x] = s;
+}
+
+// blockIdx.y selects a group of (at most) eight columns, so the groups run
+// side by side and each FMA issued is needed
 template <int PASS>
 __global__ void __launch_bounds__(256)
 k_gm_dots(int n, int k, const double *__restrict__ V, size_t ldv,
@@ -480,20 +501,17 @@ k_gm_dots(int n, int k, const double *__restrict__ V, size_t ldv,
 {
   if(!S->cycle || (PASS == 1 && !S->reorth)) return;
   const int kk = PASS == 0 ? k + 1 : k;  // column k: V_k = w itself
-  for(int j0 = 0; j0 < kk; j0 += 8) {
-    double acc[8];
-#pragma unroll
-    for(int u = 0; u < 8; u++) acc[u] = 0.;
-    for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-        i += (long long)gridDim.x * blockDim.x) {
-      double wi = w[i];
-#pragma unroll
-      for(int u = 0; u < 8; u++)
-        if(j0 + u < kk) acc[u] += V[(size_t)(j0 + u) * ldv + i] * wi;
-    }
-    double s = block_sum8<256>(acc);
-    if(threadIdx.x < 8 && j0 + (int)threadIdx.x < kk)
-      part[(size_t)(j0 + threadIdx.x) * kReduceBlocks + blockIdx.x] = s;
+  const int j0 = blockIdx.y * 8;
+  if(j0 >= kk) return;
+  switch(kk - j0 < 8 ? kk - j0 : 8) {
+  case 1: dots_group<1>(n, j0, V, ldv, w, part); break;
+  case 2: dots_group<2>(n, j0, V, ldv, w, part); break;
+  case 3: dots_group<3>(n, j0, V, ldv, w, part); break;
+  case 4: dots_group<4>(n, j0, V, ldv, w, part); break;
+  case 5: dots_group<5>(n, j0, V, ldv, w, part); break;
+  case 6: dots_group<6>(n, j0, V, ldv, w, part); break;
+  case 7: dots_group<7>(n, j0, V, ldv, w, part); break;
+  default: dots_group<8>(n, j0, V, ldv, w, part); break;
   }
 }
 
@@ -831,11 +849,11 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
     spmv_guarded(A, val, z, w, &S->cycle, st);
     // classical Gram-Schmidt, a second pass only when the test asks for
     // it; both passes leave the partials of ||w||^2 in pn
-    k_gm_dots<0><<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S);
+    k_gm_dots<0><<<dim3(nb, (k + 1 + 7) / 8), 256, 0, st>>>(n, k, V, ldv, w, part, S);
     k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 0, nb);
     k_gm_update<1><<<nb, 256, 0, st>>>(n, k, V, ldv, w, pn, S, 0);
     k_gm_reorth_test<<<1, 256, 0, st>>>(S, pn, nb);
-    k_gm_dots<1><<<nb, 256, 0, st>>>(n, k, V, ldv, w, part, S);
+    k_gm_dots<1><<<dim3(nb, (k + 7) / 8), 256, 0, st>>>(n, k, V, ldv, w, part, S);
     k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 1, nb);
     k_gm_update<1><<<nb, 256, 0, st>>>(n, k, V, ldv, w, pn, S, 1);
     k_gm_step<<<1, 256, 0, st>>>(k, m, S, pn, nb);

@@ -184,23 +184,23 @@ k_b_dots(Chunks C, int k, const double *__restrict__ Vb, size_t ldv,
          const double *__restrict__ w, double *__restrict__ part, BView V)
 {
   const int kk = PASS == 0 ? k + 1 : k;
+  const int j0 = blockIdx.y * 8;  // this CTA's group of (at most) 8 columns
+  if(j0 >= kk) return;
+  const int cnt = kk - j0 < 8 ? kk - j0 : 8;
   for(int c = blockIdx.x; c < C.n; c += gridDim.x) {
     const BState &s = V.S[C.sys[c]];
     if(!s.cycle || (PASS == 1 && !s.reorth)) continue;
-    for(int j0 = 0; j0 < kk; j0 += 8) {
-      double acc[8];
+    double acc[8];
 #pragma unroll
-      for(int u = 0; u < 8; u++) acc[u] = 0.;
-      for(int i = C.r0[c] + threadIdx.x; i < C.r1[c]; i += blockDim.x) {
-        double wi = w[i];
+    for(int u = 0; u < 8; u++) acc[u] = 0.;
+    for(int i = C.r0[c] + threadIdx.x; i < C.r1[c]; i += blockDim.x) {
+      double wi = w[i];
 #pragma unroll
-        for(int u = 0; u < 8; u++)
-          if(j0 + u < kk) acc[u] += Vb[(size_t)(j0 + u) * ldv + i] * wi;
-      }
-      double s = block_sum8<kBThreads>(acc);
-      if(threadIdx.x < 8 && j0 + (int)threadIdx.x < kk)
-        part[(size_t)(j0 + threadIdx.x) * C.n + c] = s;
+      for(int u = 0; u < 8; u++)
+        if(u < cnt) acc[u] += Vb[(size_t)(j0 + u) * ldv + i] * wi;
     }
+    double t = block_sum8<kBThreads>(acc);
+    if((int)threadIdx.x < cnt) part[(size_t)(j0 + threadIdx.x) * C.n + c] = t;
   }
 }
 
@@ -578,11 +578,13 @@ int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
     double *z = flexible ? Z + (size_t)(k - 1) * ldv : zt;
     precond_apply(vk, z, flags.p, 0);
     k_b_spmv<2><<<gchunks, kBThreads, 0, st>>>(C, A->rowptr.p, A->col.p, val, z, w, V);
-    k_b_dots<0><<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, part, V);
+    k_b_dots<0><<<dim3(gchunks, (k + 1 + 7) / 8), kBThreads, 0, st>>>(C, k, Vb, ldv, w,
+                                                                      part, V);
     k_b_reduce<<<gwarp, 256, 0, st>>>(nsys, k, C, part, V, 0);
     k_b_update<1><<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, pn, V, 0);
     k_b_reorth_test<<<gsys, 128, 0, st>>>(nsys, C, pn, V);
-    k_b_dots<1><<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, part, V);
+    k_b_dots<1><<<dim3(gchunks, (k + 7) / 8), kBThreads, 0, st>>>(C, k, Vb, ldv, w, part,
+                                                                  V);
     k_b_reduce<<<gwarp, 256, 0, st>>>(nsys, k, C, part, V, 1);
     k_b_update<1><<<gchunks, kBThreads, 0, st>>>(C, k, Vb, ldv, w, pn, V, 1);
     k_b_step<<<gsys, 128, 0, st>>>(nsys, k, C, pn, V);
