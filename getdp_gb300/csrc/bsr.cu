@@ -483,8 +483,10 @@ k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
 // flight per lane, streaming loads, CTAs per SM the registers must allow):
 // 0 (8,2,cs) 1 (8,2,ldg) 2 (16,2,cs) 3 (16,2,ldg) 4 (8,4,ldg) 5 (32,2,ldg);
 // 6 and 7: the TMA-staged kernel with 16 and 8 lanes per block row;
-// 8 (8,2,ldg,8 CTAs) 9 (8,4,ldg,4 CTAs) 10 (8,2,ldg,4 CTAs)
-constexpr int kBsrVariants = 11;
+// 8 (8,2,ldg,8 CTAs) 9 (8,4,ldg,4 CTAs) 10 (8,2,ldg,4 CTAs); fewer lanes
+// per block row, for the FP64 product whose shuffle-add tree and idle lanes
+// load GB300's FP64 pipe: 11 (4,2,ldg) 12 (4,4,ldg) 13 (2,4,ldg)
+constexpr int kBsrVariants = 14;
 
 template <int MODE, typename T, int LPR>
 static void launch_tma(const Bsr3 &B, const T *val, const T *p, const T *b,
@@ -533,6 +535,9 @@ static void launch_bsr(int variant, const Bsr3 &B, const T *val, const T *p,
   case 8: GB_BSR(8, 2, 0, 8); break;
   case 9: GB_BSR(8, 4, 0, 4); break;
   case 10: GB_BSR(8, 2, 0, 4); break;
+  case 11: GB_BSR(4, 2, 0, 0); break;
+  case 12: GB_BSR(4, 4, 0, 0); break;
+  case 13: GB_BSR(2, 4, 0, 0); break;
   default: GB_BSR(8, 2, 1, 0); break;
   }
 #undef GB_BSR
@@ -695,10 +700,11 @@ int bsr_tune(gb300_matrix *A, Bsr3 &B, cudaStream_t st, bool tune64)
   }
   if(B.val64.p) {
     // FP64 products that only recompute a residual now and then keep the
-    // default shape; tuning them would cost more than it saves
+    // default shape (4 lanes per block row: the FP64 pipe, not the memory,
+    // limits wider lane groups); tuning them would cost more than it saves
     if(A->bsr_var64 < 0 && tune64)
       GB_TRY(tune_cached<double>(B, B.val64.p, &A->bsr_var64, st));
-    B.var64 = A->bsr_var64 < 0 ? 1 : A->bsr_var64;
+    B.var64 = A->bsr_var64 < 0 ? 11 : A->bsr_var64;
   }
   return GB300_OK;
 }
