@@ -7,7 +7,10 @@
 // rows whose lower (resp. upper) neighbours all belong to earlier levels,
 // so its rows are independent.  Narrow levels (<= kNarrow rows) run back to
 // back inside one thread block separated by __syncthreads; a wide level gets
-// its own grid launch.  The triangular solves follow lusol
+// its own grid launch.  For the solves, each wide level also keeps its rows'
+// L (resp. U) entries in a sliced-ELL copy (32 rows per slice, entry j of
+// the slice's rows side by side), so that a warp reads them coalesced and
+// without the row-pointer indirection.  The triangular solves follow lusol
 // (ilut.F:2297-2347) row by row in the same accumulation order.
 //
 // GMRES(m) and FGMRES(m) follow iters.f:1912-2219 / :2522-2806 with right
@@ -35,8 +38,23 @@ struct Segment {
   int r0;      // first index in the level-row list
 };
 
+// sliced-ELL copy of one triangular part, wide levels only: slice s holds
+// 32 rows x width[s] entries at 32 * wscan[s], entry j of lane l at
+// + 32 j + l; src is the entry's position in the CSR factor (-1: padding,
+// col = the row itself with value 0)
+struct EllPart {
+  std::vector<int> slice0;  // per segment: its first slice (wide segments)
+  int nslices = 0;
+  long long entries = 0;
+  DevBuf<int> width, col, src;
+  DevBuf<long long> wscan;
+  DevBuf<double> v64;
+  DevBuf<float> v32;
+};
+
 struct ilu_data {
   int n = 0;
+  EllPart lell, uell;
   DevBuf<int> diag;                 // position of a_ii in each row
   DevBuf<int> lrows, urows;         // rows grouped by level
   DevBuf<int> lptr, uptr;           // level offsets (device copies)
@@ -160,6 +178,113 @@ static int make_levels(gb300_matrix *A, ilu_data *L, int *d_indeg,
   return GB300_OK;
 }
 
+// entries of row i's strictly lower (UPPER = 0) or upper part
+template <int UPPER>
+__device__ __forceinline__ void part_range(int i, const int *rowptr, const int *diag,
+                                           int &k0, int &cnt)
+{
+  k0 = UPPER ? diag[i] + 1 : rowptr[i];
+  cnt = UPPER ? rowptr[i + 1] - diag[i] - 1 : diag[i] - rowptr[i];
+}
+
+template <int UPPER>
+__global__ void k_ell_width(int r0, int w, int nsl, int slice0, const int *__restrict__ rows,
+                            const int *__restrict__ rowptr, const int *__restrict__ diag,
+                            int *__restrict__ width)
+{
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if(t >= nsl * 32) return;  // whole warps: nsl * 32 is a multiple of 32
+  int cnt = 0;
+  if(t < w) {
+    int k0;
+    part_range<UPPER>(rows[r0 + t], rowptr, diag, k0, cnt);
+  }
+  cnt = __reduce_max_sync(0xffffffffu, cnt);
+  if((t & 31) == 0) width[slice0 + (t >> 5)] = cnt;
+}
+
+template <int UPPER>
+__global__ void k_ell_fill(int r0, int w, int nsl, int slice0, const int *__restrict__ rows,
+                           const int *__restrict__ rowptr, const int *__restrict__ col,
+                           const int *__restrict__ diag, const int *__restrict__ width,
+                           const long long *__restrict__ wscan, int *__restrict__ ecol,
+                           int *__restrict__ esrc)
+{
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if(t >= nsl * 32) return;
+  int s = slice0 + (t >> 5), lane = t & 31;
+  long long base = 32 * wscan[s] + lane;
+  int W = width[s];
+  int i = 0, k0 = 0, cnt = 0;
+  if(t < w) {
+    i = rows[r0 + t];
+    part_range<UPPER>(i, rowptr, diag, k0, cnt);
+  }
+  for(int j = 0; j < W; j++) {
+    bool in = j < cnt;
+    ecol[base + 32LL * j] = in ? col[k0 + j] : i;
+    esrc[base + 32LL * j] = in ? k0 + j : -1;
+  }
+}
+
+template <typename T>
+__global__ void k_ell_vals(long long m, const int *__restrict__ src, const T *__restrict__ lu,
+                           T *__restrict__ v)
+{
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if(e < m) v[e] = src[e] >= 0 ? lu[src[e]] : (T)0;
+}
+
+template <int UPPER>
+static int build_ell(gb300_matrix *A, const std::vector<Segment> &seg, const int *rows,
+                     const int *diag, EllPart &E, cudaStream_t st)
+{
+  E.slice0.assign(seg.size(), -1);
+  E.nslices = 0;
+  for(size_t q = 0; q < seg.size(); q++)
+    if(!seg[q].narrow) {
+      E.slice0[q] = E.nslices;
+      E.nslices += (seg[q].width + 31) / 32;
+    }
+  E.entries = 0;
+  if(E.nslices == 0) return GB300_OK;
+  GB_TRY(E.width.alloc(E.nslices));
+  GB_TRY(E.wscan.alloc(E.nslices));
+  for(size_t q = 0; q < seg.size(); q++)
+    if(!seg[q].narrow) {
+      int nsl = (seg[q].width + 31) / 32;
+      k_ell_width<UPPER><<<grid_for((long long)nsl * 32, 256), 256, 0, st>>>(
+        seg[q].r0, seg[q].width, nsl, E.slice0[q], rows, A->rowptr.p, diag, E.width.p);
+    }
+  DevBuf<long long> tmp;
+  long long total = 0;
+  GB_TRY(exclusive_scan(E.width.p, E.nslices, E.wscan.p, &total, tmp, st));
+  E.entries = 32 * total;
+  GB_TRY(E.col.alloc(E.entries > 0 ? E.entries : 1));
+  GB_TRY(E.src.alloc(E.entries > 0 ? E.entries : 1));
+  for(size_t q = 0; q < seg.size(); q++)
+    if(!seg[q].narrow) {
+      int nsl = (seg[q].width + 31) / 32;
+      k_ell_fill<UPPER><<<grid_for((long long)nsl * 32, 256), 256, 0, st>>>(
+        seg[q].r0, seg[q].width, nsl, E.slice0[q], rows, A->rowptr.p, A->col.p, diag,
+        E.width.p, E.wscan.p, E.col.p, E.src.p);
+    }
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(st));
+  return GB300_OK;
+}
+
+// the factor's values in the ELL copies (after each factorisation)
+template <typename T>
+static int ell_values(EllPart &E, const T *lu, DevBuf<T> &v, cudaStream_t st)
+{
+  if(E.entries == 0) return GB300_OK;
+  GB_TRY(v.alloc(E.entries));
+  k_ell_vals<T><<<grid_for(E.entries, 256), 256, 0, st>>>(E.entries, E.src.p, lu, v.p);
+  GB_CUDA(cudaGetLastError());
+  return GB300_OK;
+}
+
 static int ilu_setup(gb300_matrix *A)
 {
   if(A->ilu && A->ilu->n == A->n) return GB300_OK;
@@ -195,6 +320,8 @@ static int ilu_setup(gb300_matrix *A)
   int rc = make_levels<0>(A, L, indl.p, L->lrows, L->lptr, L->hlptr, L->lseg);
   if(rc == GB300_OK)
     rc = make_levels<1>(A, L, indu.p, L->urows, L->uptr, L->huptr, L->useg);
+  if(rc == GB300_OK) rc = build_ell<0>(A, L->lseg, L->lrows.p, L->diag.p, L->lell, st);
+  if(rc == GB300_OK) rc = build_ell<1>(A, L->useg, L->urows.p, L->diag.p, L->uell, st);
   if(rc != GB300_OK) {
     ilu_free(A->ilu);
     A->ilu = nullptr;
@@ -305,6 +432,34 @@ k_level_wide(int r0, int width, const int *__restrict__ rows,
     row_bwd<T>(i, rowptr, col, diag, lu, inv, x);
 }
 
+// one wide level of a triangular solve from the sliced-ELL copy: entry j
+// of the warp's 32 rows is one coalesced load (the row's entries stay in
+// CSR order, the accumulation order of lusol)
+template <int MODE, typename T>
+__global__ void __launch_bounds__(256)
+k_level_ell(int r0, int w, int slice0, const int *__restrict__ rows,
+            const int *__restrict__ width, const long long *__restrict__ wscan,
+            const int *__restrict__ ecol, const T *__restrict__ ev,
+            const T *__restrict__ inv, T *x, const int *flag,
+            const unsigned char *__restrict__ rmask)
+{
+  if(flag && !*flag) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if(t >= w) return;
+  int i = rows[r0 + t];
+  if(rmask && !rmask[i]) return;
+  int s = slice0 + (t >> 5);
+  long long e = 32 * wscan[s] + (t & 31);
+  int W = width[s];
+  T acc = x[i];
+  for(int j = 0; j < W; j++, e += 32) acc = acc - ev[e] * x[ecol[e]];
+  x[i] = (MODE == 2) ? inv[i] * acc : acc;
+}
+
+template <typename T> const T *ell_vals(const EllPart &E);
+template <> const double *ell_vals<double>(const EllPart &E) { return E.v64.p; }
+template <> const float *ell_vals<float>(const EllPart &E) { return E.v32.p; }
+
 // rmask (sweeps only): rows with rmask[i] == 0 are skipped (the rows of
 // systems of a batch that have stopped)
 template <int MODE, typename T>
@@ -316,7 +471,15 @@ static void run_levels(const gb300_matrix *A, const ilu_data *L, T *lu, T *inv,
   const std::vector<Segment> &seg = upper ? L->useg : L->lseg;
   const int *rows = upper ? L->urows.p : L->lrows.p;
   const int *lptr = upper ? L->uptr.p : L->lptr.p;
-  for(const Segment &s : seg) {
+  const EllPart &E = upper ? L->uell : L->lell;
+  for(size_t q = 0; q < seg.size(); q++) {
+    const Segment &s = seg[q];
+    if(MODE != 0 && !s.narrow && E.entries > 0) {
+      k_level_ell<MODE, T><<<grid_for(s.width, 256), 256, 0, st>>>(
+        s.r0, s.width, E.slice0[q], rows, E.width.p, E.wscan.p, E.col.p,
+        ell_vals<T>(E), inv, x, flag, rmask);
+      continue;
+    }
     if(s.narrow)
       k_levels_narrow<MODE, T><<<1, kNarrowThreads, 0, st>>>(
         s.l0, s.l1, lptr, rows, A->rowptr.p, A->col.p, L->diag.p, lu, inv, x,
@@ -355,6 +518,8 @@ int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out)
                             cudaMemcpyDeviceToDevice, st));
     run_levels<0, double>(A, L, L->lu64.p, L->inv64.p, (double *)nullptr, zr.p,
                           nullptr, st);
+    GB_TRY(ell_values<double>(L->lell, L->lu64.p, L->lell.v64, st));
+    GB_TRY(ell_values<double>(L->uell, L->lu64.p, L->uell.v64, st));
   }
   else {
     GB_TRY(L->lu32.alloc(A->nnz));
@@ -363,6 +528,8 @@ int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out)
                                                                 L->lu32.p, nullptr);
     run_levels<0, float>(A, L, L->lu32.p, L->inv32.p, (float *)nullptr, zr.p,
                          nullptr, st);
+    GB_TRY(ell_values<float>(L->lell, L->lu32.p, L->lell.v32, st));
+    GB_TRY(ell_values<float>(L->uell, L->lu32.p, L->uell.v32, st));
   }
   int hz = 0;
   GB_CUDA(cudaMemcpyAsync(&hz, zr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
