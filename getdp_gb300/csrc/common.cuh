@@ -165,7 +165,7 @@ __device__ __forceinline__ bool arrive_last(unsigned *counter)
   __syncthreads();
   if(threadIdx.x == 0) {
     unsigned t = atomicAdd(counter, 1u);
-    last = (t == gridDim.x - 1);
+    last = (t == gridDim.x * gridDim.y * gridDim.z - 1);
     if(last) *counter = 0u;
   }
   __syncthreads();

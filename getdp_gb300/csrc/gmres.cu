@@ -591,6 +591,8 @@ struct GmState {
   double nrm0;      // ||w||^2 before the Gram-Schmidt pass of this step
   int reorth;       // this step takes a second Gram-Schmidt pass
   int reorths;      // second passes taken so far
+  // arrival counters of the kernels whose last CTA finishes a reduction
+  unsigned tick_dots0, tick_dots1, tick_upd0, tick_upd1;
 };
 
 // restart: r = rhs - A x was computed with its partial norms
@@ -658,110 +660,10 @@ __device__ __forceinline__ void dots_group(int n, int j0, const double *__restri
   if(threadIdx.x < CNT) part[(size_t)(j0 + threadIdx.x) * kReduceBlocks + blockIdx.x] = s;
 }
 
-// blockIdx.y selects a group of (at most) eight columns, so the groups run
-// side by side and each FMA issued is needed
-template <int PASS>
-__global__ void __launch_bounds__(256)
-k_gm_dots(int n, int k, const double *__restrict__ V, size_t ldv,
-          const double *__restrict__ w, double *__restrict__ part,
-          const GmState *__restrict__ S)
+// end of one Arnoldi step (thread 0), with rr = ||w||^2 after the
+// Gram-Schmidt pass: h(k+1,k), Givens rotations, stopping test
+__device__ void gm_step_tail(GmState *S, int k, int m, double rr)
 {
-  if(!S->cycle || (PASS == 1 && !S->reorth)) return;
-  const int kk = PASS == 0 ? k + 1 : k;  // column k: V_k = w itself
-  const int j0 = blockIdx.y * 8;
-  if(j0 >= kk) return;
-  switch(kk - j0 < 8 ? kk - j0 : 8) {
-  case 1: dots_group<1>(n, j0, V, ldv, w, part); break;
-  case 2: dots_group<2>(n, j0, V, ldv, w, part); break;
-  case 3: dots_group<3>(n, j0, V, ldv, w, part); break;
-  case 4: dots_group<4>(n, j0, V, ldv, w, part); break;
-  case 5: dots_group<5>(n, j0, V, ldv, w, part); break;
-  case 6: dots_group<6>(n, j0, V, ldv, w, part); break;
-  case 7: dots_group<7>(n, j0, V, ldv, w, part); break;
-  default: dots_group<8>(n, j0, V, ldv, w, part); break;
-  }
-}
-
-// h[j] = sum of partials (one warp per j); pass 0 stores h1 (and the
-// column of H) and ||w||^2, pass 1 stores h2 and adds it to the column
-__global__ void k_gm_reduce(int k, const double *__restrict__ part, GmState *S,
-                            int pass, int nb)
-{
-  if(!S->cycle || (pass == 1 && !S->reorth)) return;
-  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int kk = pass == 0 ? k + 1 : k;
-  for(int j = w; j < kk; j += blockDim.x / 32) {
-    double v = 0.;
-    for(int b = lane; b < nb; b += 32) v += part[(size_t)j * kReduceBlocks + b];
-    v = warp_sum(v);
-    if(lane == 0) {
-      if(j == k)
-        S->nrm0 = v;
-      else if(pass == 0) {
-        S->h1[j] = v;
-        S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = v;
-      }
-      else {
-        S->h2[j] = v;
-        S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = S->h1[j] + v;
-      }
-    }
-  }
-}
-
-// Selective re-orthogonalisation with mgsro's constant (iters.f:3475-3600,
-// reorth = 0.98): mgsro repeats the projection on one basis vector when it
-// removed more than 98 % of the squared norm left; here the second
-// classical Gram-Schmidt pass runs when the first pass removed more than
-// 98 % of ||w||^2 (||w'|| < 0.14 ||w||).  The loss of orthogonality of one
-// pass grows like eps ||w|| / ||w'||, so a pass that keeps more than 2 % of
-// ||w||^2 leaves w' orthogonal to within ~10 eps.
-__global__ void k_gm_reorth_test(GmState *S, const double *__restrict__ pn, int nb)
-{
-  if(!S->cycle) return;
-  double rr = 0.;
-  for(int i = threadIdx.x; i < nb; i += blockDim.x) rr += pn[i];
-  rr = block_sum<double, 256>(rr);
-  if(threadIdx.x) return;
-  S->reorth = !(rr >= 0.02 * S->nrm0);
-  if(S->reorth) S->reorths += 1;
-}
-
-// w -= sum_j h_j V_j (h from pass `pass`); with NORM the partial ||w||^2
-template <int NORM>
-__global__ void __launch_bounds__(256)
-k_gm_update(int n, int k, const double *__restrict__ V, size_t ldv,
-            double *__restrict__ w, double *__restrict__ part,
-            const GmState *__restrict__ S, int pass)
-{
-  if(!S->cycle || (pass == 1 && !S->reorth)) return;
-  __shared__ double h[kMaxKrylov];
-  for(int j = threadIdx.x; j < k; j += blockDim.x)
-    h[j] = pass == 0 ? S->h1[j] : S->h2[j];
-  __syncthreads();
-  double v = 0.;
-  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-      i += (long long)gridDim.x * blockDim.x) {
-    double wi = w[i];
-    for(int j = 0; j < k; j++) wi -= h[j] * V[(size_t)j * ldv + i];
-    w[i] = wi;
-    v += wi * wi;
-  }
-  if(NORM) {
-    double s = block_sum<double, 256>(v);
-    if(threadIdx.x == 0) part[blockIdx.x] = s;
-  }
-}
-
-// end of one Arnoldi step: h(k+1,k), Givens rotations, stopping test
-__global__ void k_gm_step(int k, int m, GmState *S, const double *__restrict__ part,
-                          int nb)
-{
-  if(!S->cycle) return;
-  double rr = 0.;
-  for(int i = threadIdx.x; i < nb; i += blockDim.x) rr += part[i];
-  rr = block_sum<double, 256>(rr);
-  if(threadIdx.x) return;
   S->its += 1;
   double *Hc = S->H + (size_t)(k - 1) * (kMaxKrylov + 1);  // column k
   double nrm = sqrt(rr);
@@ -791,6 +693,98 @@ __global__ void k_gm_step(int k, int m, GmState *S, const double *__restrict__ p
   S->scale = 1. / nrm;
   if(!(k < m && !(alpha <= S->tol) && (S->maxit <= 0 || S->its < S->maxit)))
     S->cycle = 0;  // end of this cycle after the scaling below is skipped
+}
+
+// Partial dots <V_j, w>, j < k, over a fixed grid (part[j * B + block]);
+// blockIdx.y selects a group of (at most) eight columns, so the groups run
+// side by side and each FMA issued is needed.  PASS 0 also forms <w, w>
+// (column k: V_k is w), the norm the selective re-orthogonalisation
+// compares with; PASS 1 runs only when this step takes the second pass.
+// The last CTA to finish sums the partials in a fixed order (one warp per
+// column): PASS 0 stores h1 (and the column of H) and ||w||^2, PASS 1
+// stores h2 and adds it to the column.
+template <int PASS>
+__global__ void __launch_bounds__(256)
+k_gm_dots(int n, int k, const double *__restrict__ V, size_t ldv,
+          const double *__restrict__ w, double *__restrict__ part, GmState *S, int nb)
+{
+  if(!S->cycle || (PASS == 1 && !S->reorth)) return;  // the same in every CTA
+  const int kk = PASS == 0 ? k + 1 : k;  // column k: V_k = w itself
+  const int j0 = blockIdx.y * 8;
+  switch(j0 >= kk ? 0 : kk - j0 < 8 ? kk - j0 : 8) {
+  case 0: break;
+  case 1: dots_group<1>(n, j0, V, ldv, w, part); break;
+  case 2: dots_group<2>(n, j0, V, ldv, w, part); break;
+  case 3: dots_group<3>(n, j0, V, ldv, w, part); break;
+  case 4: dots_group<4>(n, j0, V, ldv, w, part); break;
+  case 5: dots_group<5>(n, j0, V, ldv, w, part); break;
+  case 6: dots_group<6>(n, j0, V, ldv, w, part); break;
+  case 7: dots_group<7>(n, j0, V, ldv, w, part); break;
+  default: dots_group<8>(n, j0, V, ldv, w, part); break;
+  }
+  if(!arrive_last(PASS == 0 ? &S->tick_dots0 : &S->tick_dots1)) return;
+  int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for(int j = wp; j < kk; j += blockDim.x / 32) {
+    double v = 0.;
+    for(int b = lane; b < nb; b += 32) v += __ldcg(part + (size_t)j * kReduceBlocks + b);
+    v = warp_sum(v);
+    if(lane == 0) {
+      if(j == k)
+        S->nrm0 = v;
+      else if(PASS == 0) {
+        S->h1[j] = v;
+        S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = v;
+      }
+      else {
+        S->h2[j] = v;
+        S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = S->h1[j] + v;
+      }
+    }
+  }
+}
+
+// w -= sum_j h_j V_j (h of pass `pass`) with the partials of ||w||^2 in pn.
+// The last CTA to finish sums them.  After pass 0 it applies the selective
+// re-orthogonalisation test with mgsro's constant (iters.f:3475-3600,
+// reorth = 0.98: mgsro repeats the projection on one basis vector when it
+// removed more than 98 % of the squared norm left; here the second
+// classical Gram-Schmidt pass runs when the first pass removed more than
+// 98 % of ||w||^2, ||w'|| < 0.14 ||w||; the loss of orthogonality of one
+// pass grows like eps ||w|| / ||w'||, so a pass that keeps more than 2 %
+// leaves w' orthogonal to within ~10 eps) and, without a second pass, ends
+// the Arnoldi step; after pass 1 it ends the step.
+__global__ void __launch_bounds__(256)
+k_gm_update(int n, int k, int m, const double *__restrict__ V, size_t ldv,
+            double *__restrict__ w, double *__restrict__ pn, GmState *S, int pass, int nb)
+{
+  if(!S->cycle || (pass == 1 && !S->reorth)) return;  // the same in every CTA
+  __shared__ double h[kMaxKrylov];
+  for(int j = threadIdx.x; j < k; j += blockDim.x)
+    h[j] = pass == 0 ? S->h1[j] : S->h2[j];
+  __syncthreads();
+  double v = 0.;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x) {
+    double wi = w[i];
+    for(int j = 0; j < k; j++) wi -= h[j] * V[(size_t)j * ldv + i];
+    w[i] = wi;
+    v += wi * wi;
+  }
+  double s = block_sum<double, 256>(v);
+  if(threadIdx.x == 0) pn[blockIdx.x] = s;
+  if(!arrive_last(pass == 0 ? &S->tick_upd0 : &S->tick_upd1)) return;
+  double rr = 0.;
+  for(int i = threadIdx.x; i < nb; i += blockDim.x) rr += __ldcg(pn + i);
+  rr = block_sum<double, 256>(rr);
+  if(threadIdx.x) return;
+  if(pass == 0) {
+    S->reorth = !(rr >= 0.02 * S->nrm0);
+    if(S->reorth) {
+      S->reorths += 1;
+      return;  // the step ends after the second pass
+    }
+  }
+  gm_step_tail(S, k, m, rr);
 }
 
 // scale the new basis vector (runs only while the cycle continues)
@@ -1014,16 +1008,13 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
     double *z = flexible ? Z + (size_t)(k - 1) * ldv : zt;
     precond_apply(vk, z, cycle_flag(S));
     spmv_guarded(A, val, z, w, &S->cycle, st);
-    // classical Gram-Schmidt, a second pass only when the test asks for
-    // it; both passes leave the partials of ||w||^2 in pn
-    k_gm_dots<0><<<dim3(nb, (k + 1 + 7) / 8), 256, 0, st>>>(n, k, V, ldv, w, part, S);
-    k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 0, nb);
-    k_gm_update<1><<<nb, 256, 0, st>>>(n, k, V, ldv, w, pn, S, 0);
-    k_gm_reorth_test<<<1, 256, 0, st>>>(S, pn, nb);
-    k_gm_dots<1><<<dim3(nb, (k + 7) / 8), 256, 0, st>>>(n, k, V, ldv, w, part, S);
-    k_gm_reduce<<<1, 256, 0, st>>>(k, part, S, 1, nb);
-    k_gm_update<1><<<nb, 256, 0, st>>>(n, k, V, ldv, w, pn, S, 1);
-    k_gm_step<<<1, 256, 0, st>>>(k, m, S, pn, nb);
+    // classical Gram-Schmidt, a second pass only when the test after the
+    // first asks for it; the reductions, the test and the end of the step
+    // run in the last CTA of each kernel
+    k_gm_dots<0><<<dim3(nb, (k + 1 + 7) / 8), 256, 0, st>>>(n, k, V, ldv, w, part, S, nb);
+    k_gm_update<<<nb, 256, 0, st>>>(n, k, m, V, ldv, w, pn, S, 0, nb);
+    k_gm_dots<1><<<dim3(nb, (k + 7) / 8), 256, 0, st>>>(n, k, V, ldv, w, part, S, nb);
+    k_gm_update<<<nb, 256, 0, st>>>(n, k, m, V, ldv, w, pn, S, 1, nb);
     k_gm_scale_next<<<gs, 256, 0, st>>>(n, S, w, k);
   }
   k_gm_solve_small<<<1, 32, 0, st>>>(S);
