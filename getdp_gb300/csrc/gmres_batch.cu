@@ -24,7 +24,7 @@ namespace gb {
 
 // rows per chunk: per-chunk work (the system's flags, h into shared memory,
 // the block reductions) is amortised over the rows, while enough chunks
-// remain to balance the CTAs; measured on 512 systems of 961..50,562 rows:
+// remain to balance the CTAs; measured on 512 systems of 1,922..50,562 rows:
 // 512 rows 290, 2048 319, 4096 309, 8192 267 solves/s
 constexpr int kBChunk = 2048;
 constexpr int kBThreads = 256;
