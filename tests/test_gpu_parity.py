@@ -370,3 +370,73 @@ def test_multicolour_fgmres_curlcurl_backward_error():
     res_oracle = np.linalg.norm(d["b"] - Am @ xo)
     target = kw["stopping_test"] * np.linalg.norm(d["b"])
     assert res <= 20 * max(res_oracle, target), (res, res_oracle, target)
+
+
+# ---- wide levels: the sliced-ELL sweeps ---------------------------------
+# The golden systems are small: every level of their triangular solves fits
+# the one-block kernel.  A 5-point Laplacian with its rows in red-black
+# order has two levels per sweep of m^2 / 2 rows each, so the wide-level
+# (sliced-ELL) kernels run, in GetDP's order the oracle also follows.
+def _red_black_laplacian(m, shift=1e-2):
+    import scipy.sparse as sp
+    T = sp.diags([-np.ones(m - 1), 2 * np.ones(m), -np.ones(m - 1)], [-1, 0, 1])
+    A = (sp.kron(sp.identity(m), T) + sp.kron(T, sp.identity(m)) +
+         shift * sp.identity(m * m)).tocsr()
+    ii, jj = np.divmod(np.arange(m * m), m)
+    perm = np.concatenate([np.flatnonzero((ii + jj) % 2 == 0),
+                           np.flatnonzero((ii + jj) % 2 == 1)])
+    P = A[perm][:, perm].tocsr()
+    P.sort_indices()
+    return P
+
+
+@pytest.mark.parametrize("algorithm,precision,ilu", [(8, 0, "64"), (9, 1, "32")])
+def test_wide_levels_match_oracle(algorithm, precision, ilu):
+    A = _red_black_laplacian(90)  # two levels of 4,050 rows per sweep
+    n = A.shape[0]
+    rng = np.random.default_rng(11)
+    bv = rng.standard_normal(n)
+    G2 = LA.LinAlg_CreateMatrix(None, n)
+    G2.set_csr(A.indptr, A.indices, A.data)
+    b = LA.LinAlg_CreateVector(None, n)
+    b.set(bv)
+    x = LA.LinAlg_CreateVector(None, n)
+    par = {"Algorithm": algorithm, "Preconditioner": 6, "Krylov_Size": 30,
+           "Renumbering_Technique": 0, "Stopping_Test": "1e-12", "Nb_Iter_Max": 5000,
+           "Precision": precision}
+    info = LA.LinAlg_Solve(G2, b, _solver(par), x)
+    xo, st, its, _ = oracle.solve(A.indptr, A.indices, A.data, bv, algorithm=algorithm,
+                                  preconditioner=6, renumbering=0, krylov_size=30,
+                                  stopping_test=float(np.float32(1e-12)),
+                                  nb_iter_max=5000, ilu=ilu)
+    assert st == 0 and info["status"] == 0, (info, st)
+    assert abs(info["iterations"] - its) <= 0.05 * its + 2, (info, its)
+    assert np.linalg.norm(x.numpy() - xo) <= 1e-9 * np.linalg.norm(xo)
+
+
+def test_wide_levels_batched_match_single():
+    import scipy.sparse as sp
+    A1 = _red_black_laplacian(72)
+    A2 = _red_black_laplacian(66, shift=5e-2)  # levels of 2,592 and 2,178 rows
+    A = sp.block_diag([A1, A2]).tocsr()
+    A.sort_indices()
+    n1, n = A1.shape[0], A.shape[0]
+    rng = np.random.default_rng(5)
+    bv = rng.standard_normal(n)
+    G2 = LA.LinAlg_CreateMatrix(None, n)
+    G2.set_csr(A.indptr, A.indices, A.data)
+    b = LA.LinAlg_CreateVector(None, n)
+    b.set(bv)
+    x = LA.LinAlg_CreateVector(None, n)
+    par = {"Algorithm": 8, "Preconditioner": 6, "Krylov_Size": 20,
+           "Renumbering_Technique": 0, "Stopping_Test": "1e-12", "Nb_Iter_Max": 5000}
+    infos = LA.LinAlg_SolveBatch(G2, b, _solver(par), x, np.array([0, n1, n]))
+    xs = x.numpy()
+    for k, (Ak, lo, hi) in enumerate([(A1, 0, n1), (A2, n1, n)]):
+        xo, st, its, _ = oracle.solve(Ak.indptr, Ak.indices, Ak.data, bv[lo:hi],
+                                      algorithm=8, preconditioner=6, renumbering=0,
+                                      krylov_size=20, stopping_test=float(np.float32(1e-12)),
+                                      nb_iter_max=5000)
+        assert st == 0 and infos[k]["status"] == 0, (k, infos[k], st)
+        assert abs(infos[k]["iterations"] - its) <= 0.05 * its + 2, (k, infos[k], its)
+        assert np.linalg.norm(xs[lo:hi] - xo) <= 1e-9 * np.linalg.norm(xo)
