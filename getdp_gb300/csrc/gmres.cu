@@ -765,8 +765,18 @@ k_gm_update(int n, int k, int m, const double *__restrict__ V, size_t ldv,
   double v = 0.;
   for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
       i += (long long)gridDim.x * blockDim.x) {
-    double wi = w[i];
-    for(int j = 0; j < k; j++) wi -= h[j] * V[(size_t)j * ldv + i];
+    // four partial sums of h_j V_j: four independent FMA chains instead of
+    // one (the FP64 FMA latency otherwise serialises the k terms)
+    double s0 = 0., s1 = 0., s2 = 0., s3 = 0.;
+    int j = 0;
+    for(; j + 3 < k; j += 4) {
+      s0 += h[j] * V[(size_t)j * ldv + i];
+      s1 += h[j + 1] * V[(size_t)(j + 1) * ldv + i];
+      s2 += h[j + 2] * V[(size_t)(j + 2) * ldv + i];
+      s3 += h[j + 3] * V[(size_t)(j + 3) * ldv + i];
+    }
+    for(; j < k; j++) s0 += h[j] * V[(size_t)j * ldv + i];
+    double wi = w[i] - ((s0 + s1) + (s2 + s3));
     w[i] = wi;
     v += wi * wi;
   }

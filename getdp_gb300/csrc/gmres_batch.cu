@@ -249,8 +249,17 @@ k_b_update(Chunks C, int k, const double *__restrict__ Vb, size_t ldv,
     __syncthreads();
     double v = 0.;
     for(int i = C.r0[c] + threadIdx.x; i < C.r1[c]; i += blockDim.x) {
-      double wi = w[i];
-      for(int j = 0; j < k; j++) wi -= h[j] * Vb[(size_t)j * ldv + i];
+      // four independent FMA chains (see gmres.cu, k_gm_update)
+      double s0 = 0., s1 = 0., s2 = 0., s3 = 0.;
+      int j = 0;
+      for(; j + 3 < k; j += 4) {
+        s0 += h[j] * Vb[(size_t)j * ldv + i];
+        s1 += h[j + 1] * Vb[(size_t)(j + 1) * ldv + i];
+        s2 += h[j + 2] * Vb[(size_t)(j + 2) * ldv + i];
+        s3 += h[j + 3] * Vb[(size_t)(j + 3) * ldv + i];
+      }
+      for(; j < k; j++) s0 += h[j] * Vb[(size_t)j * ldv + i];
+      double wi = w[i] - ((s0 + s1) + (s2 + s3));
       w[i] = wi;
       v += wi * wi;
     }
