@@ -17,11 +17,12 @@
 // preconditioning (Preconditioner_Position 2): restart residual, Arnoldi
 // steps, Givens rotations (iters.f:3235-3273), the stopping test on the
 // Givens residual estimate, and the triangular solve + update at the end of
-// a cycle.  The orthogonalisation is classical Gram-Schmidt applied twice
-// (two passes of block dot products), which parallelises over the basis,
-// in place of the reference's sequential modified Gram-Schmidt with
-// selective re-orthogonalisation (mgsro, iters.f:3475); both return an
-// orthonormal basis to working precision.
+// a cycle.  The orthogonalisation is classical Gram-Schmidt with block dot
+// products, which parallelises over the basis, in place of the reference's
+// sequential modified Gram-Schmidt; like mgsro (iters.f:3475) it
+// re-orthogonalises selectively (a second pass when the first removed more
+// than 98 % of ||w||^2), and both return an orthonormal basis to working
+// precision.
 #include <algorithm>
 
 #include "krylov.cuh"
