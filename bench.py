@@ -502,8 +502,38 @@ def run_sweep(args, ws, rank, local):
             "sample": json.dumps({"problems": sample, "seconds": round(t_cpu, 3),
                                   "unknowns": n_sample,
                                   "extrapolated_seconds_all": round(total, 1)})}
+        # the same path on every host core: one oracle process per core,
+        # independent problems (the reference runs one system per process)
+        import multiprocessing as mp
+        cores = os.cpu_count() or 1
+        many = sorted(rng.choice(len(probs), size=min(len(probs), 4 * cores),
+                                 replace=False).tolist())
+        jobs = [(probs[k], bt.dofmaps[k]) for k in many]
+        with mp.get_context("spawn").Pool(cores) as pool:
+            pool.map(_oracle_sweep_job, jobs[:cores])  # start-up, not timed
+            t0 = time.perf_counter()
+            pool.map(_oracle_sweep_job, jobs, chunksize=1)
+            wall = time.perf_counter() - t0
+        n_many = sum(bt.dofmaps[k].n_dof for k in many)
+        total_all = wall * N / max(n_many, 1)
+        line["cpu_baseline_all_cores"] = {
+            "value": len(probs) / total_all, "unit": "solves/s", "cores": cores,
+            "kind": "port",
+            "sample": json.dumps({"problems": len(many), "seconds": round(wall, 3),
+                                  "unknowns": n_many,
+                                  "extrapolated_seconds_all": round(total_all, 1)})}
     if rank == 0:
         print(json.dumps(line))
+
+
+def _oracle_sweep_job(job):
+    """One problem of the sweep on the CPU oracle (a worker process)."""
+    import oracle
+    p, dm = job
+    ip, ix, dv, bb = oracle.assemble(p, dm)
+    oracle.solve(ip, ix, dv, bb, algorithm=8, preconditioner=6, renumbering=1,
+                 krylov_size=40, stopping_test=float(np.float32(1e-10)), nb_iter_max=5000)
+    return dm.n_dof
 
 
 # adaptive relaxation factors of the Newton step (SolveJac_AdaptRelax list)
