@@ -168,3 +168,23 @@ def test_gpu_step_length_and_newton_policy():
     kinds = [s["preconditioner"] for s in pol.log]
     assert kinds[0] != "learned"
     assert all(k == "ilu0 (learned off)" for k in kinds[1:]), kinds
+
+
+def test_committed_weights_fit_the_network():
+    # the weights that getdp_gb300/weights/train_nl2d.py produced: one
+    # parameter vector of the network's layout, finite, with a non-zero head
+    import os
+    import importlib
+    w = np.load(os.path.join(os.path.dirname(__file__), "..", "getdp_gb300", "weights",
+                             "mpnn_nl2d_256.npy"))
+    assert w.dtype == np.float32 and w.shape == (M.NPARAM,)
+    assert np.all(np.isfinite(w))
+    assert np.any(w[M.OFF_WO:M.OFF_CO] != 0)  # trained: the output head moved off zero
+    # the network's forward pass (the oracle's) runs on them
+    rng = np.random.default_rng(0)
+    n = 12
+    A = sp.diags([-np.ones(n - 1), 2.5 * np.ones(n), -np.ones(n - 1)], [-1, 0, 1]).tocsr()
+    g = M.graph(A.indptr, A.indices, A.data)
+    out = M.forward(w, g)
+    assert np.all(np.isfinite(np.asarray(out[0] if isinstance(out, tuple) else out)))
+    importlib.import_module("getdp_gb300.weights.train_nl2d")
