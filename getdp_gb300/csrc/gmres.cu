@@ -616,8 +616,11 @@ __global__ void k_gm_restart(GmState *S, const double *__restrict__ part, int m)
   S->k = 0;
   S->did_cycle = 0;
   S->breakdown = 0;
-  if(!(alpha > S->tol)) {  // converged (also for a zero right-hand side)
-    S->status = (alpha == alpha) ? 0 : -10;
+  // iters.f's restart test: converged when alpha <= tol (also for a zero
+  // right-hand side); a NaN residual goes on to the Arnoldi step, where the
+  // abnormal norm ends the solve as a break-down
+  if(alpha <= S->tol) {
+    S->status = 0;
     S->res6 = alpha;
     S->active = 0;
     S->cycle = 0;
@@ -724,22 +727,42 @@ k_gm_dots(int n, int k, const double *__restrict__ V, size_t ldv,
   default: dots_group<8>(n, j0, V, ldv, w, part); break;
   }
   if(!arrive_last(PASS == 0 ? &S->tick_dots0 : &S->tick_dots1)) return;
+  __shared__ double sums[kMaxKrylov + 1];
+  __shared__ int abnormal;
   int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for(int j = wp; j < kk; j += blockDim.x / 32) {
     double v = 0.;
     for(int b = lane; b < nb; b += 32) v += __ldcg(part + (size_t)j * kReduceBlocks + b);
     v = warp_sum(v);
-    if(lane == 0) {
-      if(j == k)
-        S->nrm0 = v;
-      else if(PASS == 0) {
-        S->h1[j] = v;
-        S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = v;
+    if(lane == 0) sums[j] = v;
+  }
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    abnormal = 0;
+    if(PASS == 0) {
+      // mgsro's checks on ||w||^2 before it orthogonalises (iters.f:
+      // 3475-3600): zero (ierr -1) or abnormal (-2) leaves the column
+      // unwritten and ends the cycle; gmres then reports a break-down
+      const double nrm0 = sums[k];
+      S->nrm0 = nrm0;
+      if(!(nrm0 > 0. && 1. / nrm0 > 0.)) {
+        abnormal = 1;
+        S->its += 1;  // the Arnoldi step's product was formed
+        S->breakdown = (nrm0 <= 0.) ? -1 : -2;
+        S->cycle = 0;
       }
-      else {
-        S->h2[j] = v;
-        S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = S->h1[j] + v;
-      }
+    }
+  }
+  __syncthreads();
+  if(abnormal) return;
+  for(int j = threadIdx.x; j < k; j += blockDim.x) {
+    if(PASS == 0) {
+      S->h1[j] = sums[j];
+      S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = sums[j];
+    }
+    else {
+      S->h2[j] = sums[j];
+      S->H[(size_t)(k - 1) * (kMaxKrylov + 1) + j] = S->h1[j] + sums[j];
     }
   }
 }

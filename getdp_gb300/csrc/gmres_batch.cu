@@ -156,8 +156,8 @@ __global__ void k_b_restart(int nsys, BView V, const int *__restrict__ cb,
   S.k = 0;
   S.did_cycle = 0;
   S.breakdown = 0;
-  if(!(alpha > S.tol)) {
-    S.status = (alpha == alpha) ? 0 : -10;
+  if(alpha <= S.tol) {  // the restart test of gmres.cu (iters.f)
+    S.status = 0;
     S.res6 = alpha;
     S.active = 0;
     S.cycle = 0;
@@ -279,6 +279,15 @@ __global__ void k_b_reorth_test(int nsys, Chunks C, const double *__restrict__ p
   if(p >= nsys) return;
   BState &S = V.S[p];
   if(!S.cycle) return;
+  if(!(S.nrm0 > 0. && 1. / S.nrm0 > 0.)) {
+    // mgsro's zero (-1) or abnormal (-2) norm: the cycle ends as a
+    // break-down, the step's column unused (gmres.cu, k_gm_dots)
+    S.breakdown = (S.nrm0 <= 0.) ? -1 : -2;
+    S.its += 1;
+    S.cycle = 0;
+    S.reorth = 0;
+    return;
+  }
   double rr = 0.;
   for(int c = C.cb[p]; c < C.cb[p + 1]; c++) rr += pn[c];
   S.reorth = !(rr >= 0.02 * S.nrm0);

@@ -116,10 +116,8 @@ __global__ void k_cg_start(CgState *S, const double *__restrict__ part_rr,
     S->alpha = S->beta = 0.;
     S->update = S->convert = S->final_ = S->updates = 0;
     S->tick_dot = S->tick_step = 0u;
-    if(!(rr > 0.)) {  // zero right-hand side: x = 0 solves it
-      S->active = 0;
-      S->status = 0;
-    }
+    // no test before the first step, as in iters.f's cg: a zero or
+    // abnormal right-hand side stops there at brkdn (-3 / -9), x = 0
     S->go = S->active;
   }
 }
@@ -524,11 +522,7 @@ __global__ void k_rcg_start(CgState *S, const double *__restrict__ part_rr,
     S->update = S->convert = S->final_ = 0;
     S->updates = 0;
     S->tick_dot = S->tick_step = 0u;
-    if(!(rr > 0.)) {
-      S->active = 0;
-      S->status = 0;
-    }
-    S->go = S->active;
+    S->go = S->active;  // no test before the first step (see k_cg_start)
   }
 }
 

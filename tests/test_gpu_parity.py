@@ -494,3 +494,34 @@ def test_multicolour_ordering_is_first_fit_from_last(name, bs):
         return
     assert abs(info["iterations"] - its) <= 0.05 * its + 2, (info["iterations"], its)
     assert np.linalg.norm(xg - xo) <= 1e-6 * np.linalg.norm(xo)
+
+
+# ---- abnormal right-hand sides --------------------------------------------
+@pytest.mark.parametrize("kind", ["zero", "nan", "inf"])
+@pytest.mark.parametrize("algorithm,precond,precision", [(1, 0, 0), (1, 0, 1), (8, 6, 0),
+                                                         (9, 6, 0), (9, 6, 1)])
+def test_abnormal_rhs_status_matches_oracle(kind, algorithm, precond, precision):
+    # what the reference returns for a zero, NaN or infinite right-hand side
+    # (status code, products counted, x = 0): CG stops at its first brkdn,
+    # GMRES at the restart test or at mgsro's norm check
+    d, p, dm = G.load("ms2d_n8")
+    bv = np.zeros(dm.n_dof)
+    if kind != "zero":
+        bv[:] = 1.0
+        bv[3] = np.nan if kind == "nan" else np.inf
+    A = LA.LinAlg_CreateMatrix(None, dm.n_dof)
+    A.set_csr(d["indptr"], d["indices"], d["data"])
+    b = LA.LinAlg_CreateVector(None, dm.n_dof)
+    b.set(bv)
+    x = LA.LinAlg_CreateVector(None, dm.n_dof)
+    par = {"Algorithm": algorithm, "Preconditioner": precond, "Krylov_Size": 10,
+           "Renumbering_Technique": 0, "Stopping_Test": "1e-10", "Nb_Iter_Max": 100,
+           "Precision": precision}
+    info = LA.LinAlg_Solve(A, b, _solver(par), x)
+    xo, st, its, _ = oracle.solve(d["indptr"], d["indices"], d["data"], bv,
+                                  algorithm=algorithm, preconditioner=precond,
+                                  renumbering=0, krylov_size=10, nb_iter_max=100,
+                                  stopping_test=float(np.float32(1e-10)))
+    assert info["status"] == st, (info, st, its)
+    assert info["iterations"] == its, (info, its)
+    assert not np.any(x.numpy()) and not np.any(xo)
