@@ -525,3 +525,26 @@ def test_abnormal_rhs_status_matches_oracle(kind, algorithm, precond, precision)
     assert info["status"] == st, (info, st, its)
     assert info["iterations"] == its, (info, its)
     assert not np.any(x.numpy()) and not np.any(xo)
+
+
+@pytest.mark.parametrize("algorithm,precond", [(1, 0), (8, 6), (9, 6)])
+@pytest.mark.parametrize("cap", [1, 2, 5, 17])
+def test_iteration_cap_matches_oracle(algorithm, precond, cap):
+    # Nb_Iter_Max reached: status -1, the products counted as Sparskit
+    # counts them, and the partial solution of that many steps
+    d, p, dm = G.load("ms2d_n24")
+    A = LA.LinAlg_CreateMatrix(None, dm.n_dof)
+    A.set_csr(d["indptr"], d["indices"], d["data"])
+    b = LA.LinAlg_CreateVector(None, dm.n_dof)
+    b.set(d["b"])
+    x = LA.LinAlg_CreateVector(None, dm.n_dof)
+    par = {"Algorithm": algorithm, "Preconditioner": precond, "Krylov_Size": 10,
+           "Renumbering_Technique": 0, "Stopping_Test": "1e-10", "Nb_Iter_Max": cap}
+    info = LA.LinAlg_Solve(A, b, _solver(par), x)
+    xo, st, its, _ = oracle.solve(d["indptr"], d["indices"], d["data"], d["b"],
+                                  algorithm=algorithm, preconditioner=precond,
+                                  renumbering=0, krylov_size=10, nb_iter_max=cap,
+                                  stopping_test=float(np.float32(1e-10)))
+    assert st == -1 and info["status"] == -1, (info, st)
+    assert info["iterations"] == its, (info, its)
+    assert np.linalg.norm(x.numpy() - xo) <= 1e-9 * np.linalg.norm(xo)
