@@ -548,3 +548,31 @@ def test_iteration_cap_matches_oracle(algorithm, precond, cap):
     assert st == -1 and info["status"] == -1, (info, st)
     assert info["iterations"] == its, (info, its)
     assert np.linalg.norm(x.numpy() - xo) <= 1e-9 * np.linalg.norm(xo)
+
+
+@pytest.mark.parametrize("n", [1, 5])
+@pytest.mark.parametrize("algorithm,precond", [(1, 0), (8, 6), (9, 6), (8, 0)])
+def test_tiny_systems_match_oracle(n, algorithm, precond):
+    # one and five unknowns with a restart length of 50: on one unknown
+    # GMRES's first Arnoldi vector is a multiple of the basis, which the
+    # reference reports as a break-down (-3) with the exact solution
+    import scipy.sparse as sp
+    if n == 1:
+        A = sp.csr_matrix(np.array([[2.0]]))
+    else:
+        A = sp.diags([-np.ones(n - 1), 2.5 * np.ones(n), -np.ones(n - 1)], [-1, 0, 1]).tocsr()
+    A.sort_indices()
+    bv = np.arange(1, n + 1, dtype=float)
+    G2 = LA.LinAlg_CreateMatrix(None, n)
+    G2.set_csr(A.indptr, A.indices, A.data)
+    b = LA.LinAlg_CreateVector(None, n)
+    b.set(bv)
+    x = LA.LinAlg_CreateVector(None, n)
+    par = {"Algorithm": algorithm, "Preconditioner": precond, "Krylov_Size": 50,
+           "Renumbering_Technique": 0, "Stopping_Test": "1e-10", "Nb_Iter_Max": 100}
+    info = LA.LinAlg_Solve(G2, b, _solver(par), x)
+    xo, st, its, _ = oracle.solve(A.indptr, A.indices, A.data, bv, algorithm=algorithm,
+                                  preconditioner=precond, renumbering=0, krylov_size=50,
+                                  nb_iter_max=100, stopping_test=float(np.float32(1e-10)))
+    assert info["status"] == st and info["iterations"] == its, (info, st, its)
+    assert np.linalg.norm(x.numpy() - xo) <= 1e-12 * np.linalg.norm(xo)
