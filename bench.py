@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Headline benchmark: Generate + Solve of GetDP's 3D P2 elasticity case.
 
-Workload (BASELINE configuration 2): unit cube of n^3 hexes x 6 Kuhn tets
+Workload: unit cube of n^3 hexes x 6 Kuhn tets
 with 10-node (P2) elements, n = 48: 663,552 tets, 2,709,792 unknowns,
 ~229 M nonzeros; per-element lognormal Young's modulus, Poisson 0.3,
 gravity load, face x = 0 clamped; 4-point Gauss.  Solve: Jacobi-scaled CG
@@ -817,7 +817,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64+f32", "data": "synthetic (seeded)",
-        "config": {"workload": f"3D P2 elasticity {n}^3x6 tets (configs[1]), "
+        "config": {"workload": f"3D P2 elasticity {n}^3x6 tets, "
                                "Generate + Jacobi-CG to 1e-8, FP32 SpMV in FP64 reliable updates",
                    "elements": p.mesh.n_elems, "unknowns": N, "nnz": nnz,
                    "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2, no flush"},
