@@ -727,6 +727,7 @@ def main():
         t_plain = elapsed(3, 4)
         if info_plain["status"] != 0:
             raise SystemExit(f"plain FP64 solve failed: {info_plain}")
+        x_plain = x.numpy()  # the FP64 solution, for the mixed solve's error
 
     for _ in range(args.warmup):
         step(S_mixed)
@@ -750,6 +751,12 @@ def main():
     for inf in infos:
         if inf["status"] != 0:
             raise SystemExit(f"mixed solve failed: {inf}")
+    # the mixed solution against the plain FP64 one (both to 1e-8 relative
+    # residual of the scaled system), outside the timed region
+    rel_vs_fp64 = None
+    if not args.no_plain:
+        xm = x.numpy()
+        rel_vs_fp64 = float(np.linalg.norm(xm - x_plain) / np.linalg.norm(x_plain))
 
     # e2e: element tables from pinned host memory, solution back to host
     arrays = G.term_arrays(p, dm)
@@ -827,6 +834,7 @@ def main():
         "solve_iterations": inf["iterations"], "reliable_updates": inf["refinement_steps"],
         "true_rel_residual": inf["true_residual"] / inf["rhs_norm"],
         "plain_fp64_solve_s": t_plain, "plain_fp64_iterations": info_plain["iterations"],
+        "mixed_vs_plain_fp64_rel_diff": rel_vs_fp64,
         "plain_fp64_time_to_solution_s": (t_gen_full + t_plain) if t_plain else None,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": ach / peak, "traffic": traffic,
