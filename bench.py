@@ -381,6 +381,11 @@ def run_other(args, ws, rank, local):
                                         stopping_test=par["Stopping_Test"])
         t_sol = time.perf_counter() - t0
         total = t_asm + t_sol
+        # the GPU's last solution against the oracle's (both to the same
+        # relative residual; different orderings, so not bit-equal)
+        rel_oracle = None
+        if st_ == 0:
+            rel_oracle = float(np.linalg.norm(x.numpy() - xs) / max(np.linalg.norm(xs), 1e-300))
         if st_ != 0 and its > 0:
             # capped: scale the solve to the GPU FP64 iteration count
             total = t_asm + t_sol * max(res[0]["iterations"], its) / its
@@ -390,7 +395,8 @@ def run_other(args, ws, rank, local):
                                   "solve_seconds": round(t_sol, 3),
                                   "iterations": its, "status": st_,
                                   "iteration_cap": cap,
-                                  "extrapolated": bool(st_ != 0)})}
+                                  "extrapolated": bool(st_ != 0),
+                                  "rel_diff_solution_vs_oracle": rel_oracle})}
     if rank == 0:
         print(json.dumps(line))
 
