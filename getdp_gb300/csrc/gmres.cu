@@ -368,9 +368,9 @@ template <typename T>
 __device__ __forceinline__ void row_fwd(int i, const int *__restrict__ rowptr,
                                         const int *__restrict__ col,
                                         const int *__restrict__ diag,
-                                        const T *__restrict__ lu, T *x)
+                                        const T *__restrict__ lu, const T *src, T *x)
 {
-  T s = x[i];
+  T s = src[i];  // the right-hand side's entry (src may be x itself)
   for(int k = rowptr[i]; k < diag[i]; k++) s = s - lu[k] * x[col[k]];
   x[i] = s;
 }
@@ -394,7 +394,7 @@ k_levels_narrow(int l0, int l1, const int *__restrict__ lptr,
                 const int *__restrict__ rows, const int *__restrict__ rowptr,
                 const int *__restrict__ col, const int *__restrict__ diag,
                 T *lu, T *inv, T *x, int *zero_row, const int *flag,
-                const unsigned char *__restrict__ rmask)
+                const unsigned char *__restrict__ rmask, const T *src)
 {
   if(flag && !*flag) return;
   for(int l = l0; l < l1; l++) {
@@ -405,7 +405,7 @@ k_levels_narrow(int l0, int l1, const int *__restrict__ lptr,
       if(MODE == 0)
         row_fact<T>(i, rowptr, col, diag, lu, inv, zero_row);
       else if(MODE == 1)
-        row_fwd<T>(i, rowptr, col, diag, lu, x);
+        row_fwd<T>(i, rowptr, col, diag, lu, src, x);
       else
         row_bwd<T>(i, rowptr, col, diag, lu, inv, x);
     }
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(256)
 k_level_wide(int r0, int width, const int *__restrict__ rows,
              const int *__restrict__ rowptr, const int *__restrict__ col,
              const int *__restrict__ diag, T *lu, T *inv, T *x, int *zero_row,
-             const int *flag, const unsigned char *__restrict__ rmask)
+             const int *flag, const unsigned char *__restrict__ rmask, const T *src)
 {
   if(flag && !*flag) return;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -428,7 +428,7 @@ k_level_wide(int r0, int width, const int *__restrict__ rows,
   if(MODE == 0)
     row_fact<T>(i, rowptr, col, diag, lu, inv, zero_row);
   else if(MODE == 1)
-    row_fwd<T>(i, rowptr, col, diag, lu, x);
+    row_fwd<T>(i, rowptr, col, diag, lu, src, x);
   else
     row_bwd<T>(i, rowptr, col, diag, lu, inv, x);
 }
@@ -442,7 +442,7 @@ k_level_ell(int r0, int w, int slice0, const int *__restrict__ rows,
             const int *__restrict__ width, const long long *__restrict__ wscan,
             const int *__restrict__ ecol, const T *__restrict__ ev,
             const T *__restrict__ inv, T *x, const int *flag,
-            const unsigned char *__restrict__ rmask)
+            const unsigned char *__restrict__ rmask, const T *src)
 {
   if(flag && !*flag) return;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -452,7 +452,7 @@ k_level_ell(int r0, int w, int slice0, const int *__restrict__ rows,
   int s = slice0 + (t >> 5);
   long long e = 32 * wscan[s] + (t & 31);
   int W = width[s];
-  T acc = x[i];
+  T acc = (MODE == 1) ? src[i] : x[i];
   for(int j = 0; j < W; j++, e += 32) acc = acc - ev[e] * x[ecol[e]];
   x[i] = (MODE == 2) ? inv[i] * acc : acc;
 }
@@ -464,10 +464,12 @@ template <> const float *ell_vals<float>(const EllPart &E) { return E.v32.p; }
 // rmask (sweeps only): rows with rmask[i] == 0 are skipped (the rows of
 // systems of a batch that have stopped)
 template <int MODE, typename T>
+// MODE 1 reads the right-hand side from src (x when null) and writes x
 static void run_levels(const gb300_matrix *A, const ilu_data *L, T *lu, T *inv,
                        T *x, int *zero_row, const int *flag, cudaStream_t st,
-                       const unsigned char *rmask = nullptr)
+                       const unsigned char *rmask = nullptr, const T *src = nullptr)
 {
+  if(!src) src = x;
   bool upper = (MODE == 2);
   const std::vector<Segment> &seg = upper ? L->useg : L->lseg;
   const int *rows = upper ? L->urows.p : L->lrows.p;
@@ -478,17 +480,17 @@ static void run_levels(const gb300_matrix *A, const ilu_data *L, T *lu, T *inv,
     if(MODE != 0 && !s.narrow && E.entries > 0) {
       k_level_ell<MODE, T><<<grid_for(s.width, 256), 256, 0, st>>>(
         s.r0, s.width, E.slice0[q], rows, E.width.p, E.wscan.p, E.col.p,
-        ell_vals<T>(E), inv, x, flag, rmask);
+        ell_vals<T>(E), inv, x, flag, rmask, src);
       continue;
     }
     if(s.narrow)
       k_levels_narrow<MODE, T><<<1, kNarrowThreads, 0, st>>>(
         s.l0, s.l1, lptr, rows, A->rowptr.p, A->col.p, L->diag.p, lu, inv, x,
-        zero_row, flag, rmask);
+        zero_row, flag, rmask, src);
     else
       k_level_wide<MODE, T><<<grid_for(s.width, 256), 256, 0, st>>>(
         s.r0, s.width, rows, A->rowptr.p, A->col.p, L->diag.p, lu, inv, x,
-        zero_row, flag, rmask);
+        zero_row, flag, rmask, src);
   }
 }
 
@@ -548,10 +550,10 @@ void ilu_apply(const gb300_matrix *A, bool fp32, const double *v, double *z,
   const ilu_data *L = A->ilu;
   int n = A->n;
   if(!fp32) {
-    if(v != z)
-      k_cvt<double, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, z, flag);
+    // the forward sweep reads v and writes z (no copy of v first); rows a
+    // mask leaves out are not written
     run_levels<1, double>(A, L, (double *)L->lu64.p, (double *)L->inv64.p, z,
-                          nullptr, flag, st, rmask);
+                          nullptr, flag, st, rmask, v);
     run_levels<2, double>(A, L, (double *)L->lu64.p, (double *)L->inv64.p, z,
                           nullptr, flag, st, rmask);
   }
