@@ -50,8 +50,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=None,
-                    help="cells per side (default: the workload's own size)")
+    ap.add_argument("--n", "--size", dest="n", type=int, default=None,
+                    help="cells per side (default: the workload's own size); "
+                         "--size is the spelling torchrun passes through")
     ap.add_argument("--workload", default="elasticity",
                     choices=["elasticity", "magnetostatics2d", "curlcurl", "eddysweep",
                              "nonlinear"],
@@ -121,8 +122,11 @@ def dist_setup(args):
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+        if args.impl == "gb300":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:  # the reference arm runs on the host cores only
+            dist.init_process_group("gloo")
         pg = dist
     return ws, rank, local, pg
 
