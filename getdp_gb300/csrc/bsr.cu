@@ -344,12 +344,14 @@ k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
   TmaTile<T> *stage = (TmaTile<T> *)smem_raw;
   __shared__ __align__(8) unsigned long long bar[2];
   __shared__ int tile_k0[2], tile_n[2];  // aligned first block, blocks copied
+  __shared__ int in_flight[2];  // a copy into the stage has not been waited for
   const int ntiles = (nn + kTileRows - 1) / kTileRows;
   const int tid = threadIdx.x;
 
   if(tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
+    in_flight[0] = in_flight[1] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -367,6 +369,7 @@ k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
       return;
     }
     tile_n[s] = nb;
+    in_flight[s] = 1;
     unsigned bytes = (unsigned)(9 * nb * sizeof(T) + nb * sizeof(int));
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_expect_tx(&bar[s], bytes);
@@ -398,6 +401,7 @@ k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
         break;
       }
       phase[s] ^= 1u;
+      if(tid == 0) in_flight[s] = 0;  // read again only after the next issue
     }
     int k0a = tile_k0[s];
     const T *sv = stage[s].val[0];
@@ -457,11 +461,13 @@ k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
     __syncthreads();
   }
   if(failed) {
-    // record, then let the copies still in flight land before leaving
+    // record, then let the copies still in flight land before leaving (only
+    // stages with a copy issued and not yet waited for: a stage whose tile
+    // was consumed has no phase left to complete)
     if(tid == 0) {
       atomicExch(err, 1);
       for(int s = 0; s < 2; s++)
-        if(tile_n[s] > 0) mbar_wait_bounded(&bar[s], phase[s]);
+        if(in_flight[s]) mbar_wait_bounded(&bar[s], phase[s]);
     }
     __syncthreads();
     red = 0.;  // the result is void (err is set); keep the reduction whole
@@ -561,6 +567,24 @@ void bsr_residual64(const Bsr3 &B, const double *x, const double *b, double *r,
                     double *part, const int *flag, cudaStream_t st)
 {
   launch_bsr<1, double>(B.var64, B, B.val64.p, x, b, r, part, flag, st);
+}
+
+// The staged (TMA) variants report a bulk copy that did not complete within
+// its bounded wait through B.err, leaving that product incomplete; a solve
+// that ran one of them checks the flag once at its end.
+int bsr_check(const Bsr3 &B, cudaStream_t st)
+{
+  bool staged = (B.val32.p && (B.var32 == 6 || B.var32 == 7)) ||
+                (B.val64.p && (B.var64 == 6 || B.var64 == 7));
+  if(!staged || !B.err.p) return GB300_OK;
+  int he = 0;
+  GB_CUDA(cudaMemcpyAsync(&he, B.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if(he) {
+    set_error("block SpMV: a staged copy did not complete within its wait limit");
+    return GB300_ERR_CUDA;
+  }
+  return GB300_OK;
 }
 
 template <typename T>

@@ -860,6 +860,7 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
                              p->nb_iter_max, reliable_delta(p), &hs, W));
       }
       from_nodes64(nn, x4, x, st);
+      GB_TRY(bsr_check(B, st));
     }
     else if(!mixed) {
       auto spmv = [&](const double *pp, double *qq, double *part,

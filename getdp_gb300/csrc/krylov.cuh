@@ -56,6 +56,8 @@ void bsr_spmv_dot64(const Bsr3 &B, const double *p, double *q, double *part,
                     cudaStream_t st);
 void bsr_residual64(const Bsr3 &B, const double *x, const double *b, double *r,
                     double *part, const int *flag, cudaStream_t st);
+// GB300_ERR_CUDA if a staged SpMV variant timed out during the solve
+int bsr_check(const Bsr3 &B, cudaStream_t st);
 
 // Preconditioner 20 (not a Sparskit value): ILU(0), then z += G (v - A z)
 // with G the learned correction on A's pattern (gb300_matrix_set_correction)

@@ -16,7 +16,9 @@
 //
 // Set-up: the first call on a device looks up the array's device address
 // with cudaGetSymbolAddress (with that device current) and caches it; make
-// that first call before any stream capture.  Every call shares the array:
+// that first call before any stream capture.  Every call returns the norm
+// on the host, so it waits for the context's stream to finish its work
+// before it returns.  Every call shares the array:
 // each call overwrites all the partial sums it reads, so nothing needs
 // clearing, but calls that overlap on the GPU (two streams, two threads,
 // two contexts on the same device) race on it and must be serialized by the

@@ -1,7 +1,7 @@
 // GetDP linear-algebra backend on the GB300 library: the functions of
 // src/kernel/LinAlg.h:90-213, compiled into GetDP in place of
-// src/kernel/LinAlg_SPARSKIT.cpp when HAVE_GB300 is defined (see the
-// LinAlg.h and configuration changes in INTEGRATION.md).
+// src/kernel/LinAlg_SPARSKIT.cpp when HAVE_GB300 is defined (build_getdp.sh
+// adds the HAVE_GB300 branch of LinAlg.h and the configuration define).
 //
 // Types (declared in the HAVE_GB300 branch of LinAlg.h):
 //   gMatrix { gb300_matrix *M; }            device CSR, adds staged in order

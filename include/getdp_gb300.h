@@ -284,7 +284,9 @@ int gb300_bench_spmv(gb300_matrix *A, int precision, int reps, double *ms);
    assembled and have at most 33,554,432 rows (GB300_ERR_CAPACITY
    otherwise).  The array (128 KiB) is held on every GPU that loads the
    library until the process exits.  The first call on a device looks up
-   the array's address; make it before any stream capture.  All calls share
+   the array's address; make it before any stream capture.  Each call
+   returns the norm on the host and so waits for the context's stream to
+   finish before it returns.  All calls share
    the array, so calls that overlap on the GPU race and must be serialized
    by the caller. */
 int gb300_residual_noalloc(gb300_matrix *A, const gb300_vector *x,

@@ -9,14 +9,27 @@
 #   oracle/_ref/getdp_ilu32  -- HAVE_ILU_FLOAT, as the official build
 #   oracle/_ref/getdp_ilu64  -- double-precision ILU, the strict FP64 oracle
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# The path of the sources it compiled is recorded in oracle/_ref/source_dir,
+# where the tests that read the reference's own files (examples/, src/) find
+# it (oracle/refsrc.py).
+#
+# Usage: oracle/build_ref.sh [--optional] [REFERENCE_ROOT]
+#   REFERENCE_ROOT defaults to $GETDP_SOURCE_DIR, else /root/reference (the
+#   development container); --optional exits 0 without building when the
+#   sources are absent (the GPU hosts, which get no reference sources).
 set -euo pipefail
-REF=${1:-/root/reference}
+OPTIONAL=0
+if [ "${1:-}" = "--optional" ]; then OPTIONAL=1; shift; fi
+REF=${1:-${GETDP_SOURCE_DIR:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=$HERE/_ref
 OBJ=$OUT/obj
-[ -d "$REF/src/kernel" ] || { echo "reference sources not found at $REF" >&2; exit 1; }
+if [ ! -d "$REF/src/kernel" ]; then
+  [ $OPTIONAL = 1 ] && exit 0
+  echo "reference sources not found at $REF" >&2; exit 1
+fi
 mkdir -p "$OBJ"
+echo "$REF" > "$OUT/source_dir"
 INC="-I$HERE/ref_config -I$REF/src/common -I$REF/src/kernel -I$REF/src/functions \
  -I$REF/src/interface -I$REF/src/numeric -I$REF/contrib/Sparskit"
 CXXFLAGS="-O2 -std=c++11 -w -fno-strict-aliasing"

@@ -12,10 +12,11 @@ import pytest
 
 from getdp_gb300 import fileio as FIO
 from getdp_gb300 import workloads as W
+from oracle import refsrc
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF = os.path.join(ROOT, "oracle", "_ref", "getdp_ilu64")
-GETDP_SRC = "/root/reference"
+GETDP_SRC = refsrc.source_dir() or ""
 
 
 @pytest.mark.parametrize("p", [W.magnetostatics_2d(n=9, seed=2), W.curlcurl_edge(n=3, seed=1),

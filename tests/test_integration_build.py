@@ -10,7 +10,9 @@ import subprocess
 
 import pytest
 
-GETDP_SRC = os.environ.get("GETDP_SOURCE_DIR", "/root/reference")
+from oracle import refsrc
+
+GETDP_SRC = refsrc.source_dir() or ""
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 

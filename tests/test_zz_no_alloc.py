@@ -5,14 +5,19 @@ It is called through the C ABI twice in a row (its scratch array keeps the
 previous call's contents) and each result is checked against the library's
 existing entry points -- gb300_matrix_mult for A x and gb300_vector_norm2
 for the norm -- within the tolerance the other SpMV tests use (1e-13
-relative).  This file is collected last so that a run stopping at the first
-failure has already run every other test; it also passes on its own in a
-fresh process (the first call does the per-device set-up).
+relative), and against b - A x formed on the host in FP64 by scipy (within
+1e-13 of sum_j |a_ij x_j| + |b_i|, the rounding bound of a row's dot
+product).  Further calls must leave the device's free memory unchanged,
+and an r that aliases x or b is rejected.  This file is collected last so
+that a run stopping at the first failure has already run every other test;
+it also passes on its own in a fresh process (the first call does the
+per-device set-up).
 """
 import ctypes
 
 import numpy as np
 import pytest
+import scipy.sparse as sp
 
 from getdp_gb300 import _lib
 from getdp_gb300 import linalg as LA
@@ -67,6 +72,41 @@ def test_residual_noalloc_matches_existing_entry_points(lib, name):
         scale = np.max(np.abs(r_ref))
         assert np.all(np.abs(got - r_ref) <= RTOL * (np.abs(r_ref) + scale)), call
         assert abs(nrm.value - n_ref) <= RTOL * n_ref, (call, nrm.value, n_ref)
+        # independent host product (FP64, scipy CSR)
+        M = sp.csr_matrix((d["data"], d["indices"], d["indptr"]), shape=(n, n))
+        r_host = bv - M @ xv
+        bound = abs(M) @ np.abs(xv) + np.abs(bv)
+        assert np.all(np.abs(got - r_host) <= RTOL * bound), call
+        assert abs(nrm.value - np.linalg.norm(r_host)) <= RTOL * np.linalg.norm(bound), call
+
+
+def _free_device_bytes():
+    """cudaMemGetInfo from the CUDA runtime the library is linked with."""
+    rt = ctypes.CDLL("libcudart.so.13")
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
+def test_residual_noalloc_allocates_nothing_and_rejects_aliases(lib):
+    d, p, dm = G.load("ms2d_n24")
+    n = dm.n_dof
+    A = LA.gMatrix(n)
+    A.set_csr(d["indptr"], d["indices"], d["data"])
+    x, b, r = LA.gVector(n), LA.gVector(n), LA.gVector(n)
+    x.set(np.linspace(-1.0, 1.0, n))
+    b.set(d["b"])
+    nrm = ctypes.c_double()
+    # the first call sets up the device (kernel loading, symbol lookup)
+    _lib.check(lib.gb300_residual_noalloc(A.h, x.h, b.h, r.h, ctypes.byref(nrm)))
+    free0 = _free_device_bytes()
+    for _ in range(5):
+        _lib.check(lib.gb300_residual_noalloc(A.h, x.h, b.h, r.h, ctypes.byref(nrm)))
+    assert _free_device_bytes() == free0
+    # r must be a vector of its own
+    assert lib.gb300_residual_noalloc(A.h, x.h, b.h, x.h, ctypes.byref(nrm)) == 1
+    assert b"alias" in lib.gb300_last_error()
+    assert lib.gb300_residual_noalloc(A.h, x.h, b.h, b.h, ctypes.byref(nrm)) == 1
 
 
 def test_residual_noalloc_rejects_oversized_and_unassembled(lib):
