@@ -138,6 +138,7 @@ SIGNATURES = {
     "gb300_event_record": (_I, [_P, _I]),
     "gb300_event_elapsed": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_float)]),
     "gb300_bench_spmv": (_I, [_P, _I, _I, ctypes.POINTER(_D)]),
+    "gb300_bench_fp64_peak": (_I, [_P, ctypes.POINTER(_D)]),
     "gb300_residual_noalloc": (_I, [_P, _P, _P, _P, ctypes.POINTER(_D)]),
 }
 

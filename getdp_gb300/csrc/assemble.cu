@@ -345,8 +345,8 @@ __global__ void __launch_bounds__(128)
 k_tet4_curlcurl(int ne, const double *__restrict__ nodes,
                 const int *__restrict__ elems, const int *__restrict__ edofs,
                 const signed char *__restrict__ esign,
-                const double *__restrict__ nu, const double *__restrict__ coil,
-                double reg, double J0, CsrView A, double *__restrict__ b)
+                const double *__restrict__ nu, const double *__restrict__ js,
+                double reg, CsrView A, double *__restrict__ b)
 {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if(e >= ne) return;
@@ -401,7 +401,14 @@ k_tet4_curlcurl(int ne, const double *__restrict__ nodes,
         K[t] = 4. * (F * p);
       }
   }
-  double cl = coil ? coil[e] : 0.;
+  // [ -js, {a} ] with js constant on the element: j = -js
+  double j0 = 0., j1 = 0., j2 = 0.;
+  if(js) {
+    j0 = -js[3 * e];
+    j1 = -js[3 * e + 1];
+    j2 = -js[3 * e + 2];
+  }
+  const bool cl = (j0 != 0. || j1 != 0. || j2 != 0.);
   double eb[6] = {0., 0., 0., 0., 0., 0.};
 #pragma unroll
   for(int q = 0; q < 4; q++) {
@@ -425,19 +432,10 @@ k_tet4_curlcurl(int ne, const double *__restrict__ nodes,
                    ve[i][2] * (mcoef * ve[j][2]);
         K[t] += F * p;
       }
-    if(cl != 0.) {
-      double n4[4] = {1. - u - v - w, u, v, w};
-      double X = 0., Y = 0.;
+    if(cl) {
 #pragma unroll
-      for(int i = 0; i < 4; i++) {
-        X += x[i] * n4[i];
-        Y += y[i] * n4[i];
-      }
-      double dx = X - 0.5, dy = Y - 0.5;
-      double sc = J0 / sqrt(dx * dx + dy * dy);
-      double j0 = dy * sc, j1 = -(dx * sc);  // -js = -(-(Y-0.5), X-0.5, 0)*sc
-#pragma unroll
-      for(int i = 0; i < 6; i++) eb[i] += F * (ve[i][0] * j0 + ve[i][1] * j1);
+      for(int i = 0; i < 6; i++)
+        eb[i] += F * (ve[i][0] * j0 + ve[i][1] * j1 + ve[i][2] * j2);
     }
   }
   // note: the curl-curl block is the 4-point sum of a constant, K1 = 4 F p,
@@ -454,7 +452,7 @@ k_tet4_curlcurl(int ne, const double *__restrict__ nodes,
         }
       }
   }
-  if(cl != 0.) {
+  if(cl) {
 #pragma unroll
     for(int i = 0; i < 6; i++)
       if(d[i] >= 0 && eb[i] != 0.) atomicAdd(&b[d[i]], -eb[i]);
@@ -598,7 +596,8 @@ static int stage_batch(gb300_ctx *ctx, const gb300_term_batch *t, BatchDev &B,
     GB_TRY(stage(st, t->elems, ne * nv, t->on_device, B.elems, &B.p_elems));
     GB_TRY(stage(st, t->elem_sign, ne * nloc, t->on_device, B.esign, &B.p_esign));
     GB_TRY(stage(st, t->coef, ne, t->on_device, B.coef, &B.p_coef));
-    GB_TRY(stage(st, t->source, ne, t->on_device, B.source, &B.p_source));
+    const size_t nsrc = (t->kind == GB300_TERM_TET4_EDGE_CURLCURL) ? 3 : 1;
+    GB_TRY(stage(st, t->source, ne * nsrc, t->on_device, B.source, &B.p_source));
     GB_TRY(stage(st, t->coef3, ne, t->on_device, B.coef3, &B.p_coef3));
   }
   GB_TRY(stage(st, t->coef2, ne, t->on_device, B.coef2, &B.p_coef2));
@@ -743,7 +742,7 @@ int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t,
       }
       k_tet4_curlcurl<<<grid_for(ne, 128), 128, 0, st>>>(
         ne, B.p_nodes, B.p_elems, B.p_edofs, B.p_esign, B.p_coef, B.p_source,
-        t->p0, t->p1, V, b->d.p);
+        t->p0, V, b->d.p);
       break;
     }
     GB_CUDA(cudaGetLastError());

@@ -179,12 +179,19 @@ __device__ __forceinline__ void bsr_block(const int *__restrict__ col,
 {
   int b = mload<CS>(col + k);
   auto xb = Vec4<T>::load(p + 4 * (size_t)b);
-  y0 += mload<CS>(val + k) * xb.x + mload<CS>(val + nblk + k) * xb.y +
-        mload<CS>(val + 2 * nblk + k) * xb.z;
-  y1 += mload<CS>(val + 3 * nblk + k) * xb.x + mload<CS>(val + 4 * nblk + k) * xb.y +
-        mload<CS>(val + 5 * nblk + k) * xb.z;
-  y2 += mload<CS>(val + 6 * nblk + k) * xb.x + mload<CS>(val + 7 * nblk + k) * xb.y +
-        mload<CS>(val + 8 * nblk + k) * xb.z;
+  // nine chained FMAs per block: `y += a x + b y + c z` compiles to a
+  // multiply, two FMAs and an add per row (12 FP64 instructions per block
+  // instead of 9), and GB300's FP64 pipe (2 FMAs per SM per cycle) bounds
+  // the FP64 product
+  y0 = fma(mload<CS>(val + k), xb.x, y0);
+  y1 = fma(mload<CS>(val + 3 * nblk + k), xb.x, y1);
+  y2 = fma(mload<CS>(val + 6 * nblk + k), xb.x, y2);
+  y0 = fma(mload<CS>(val + nblk + k), xb.y, y0);
+  y1 = fma(mload<CS>(val + 4 * nblk + k), xb.y, y1);
+  y2 = fma(mload<CS>(val + 7 * nblk + k), xb.y, y2);
+  y0 = fma(mload<CS>(val + 2 * nblk + k), xb.z, y0);
+  y1 = fma(mload<CS>(val + 5 * nblk + k), xb.z, y1);
+  y2 = fma(mload<CS>(val + 8 * nblk + k), xb.z, y2);
 }
 
 // MINB: CTAs per SM the register allocation must allow (0 = the compiler's
@@ -425,9 +432,15 @@ k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
             for(int c = 0; c < 9; c++) v[c] = __ldg(val + c * pstride + k);
           }
           auto xb = Vec4<T>::load(p + 4 * (size_t)b);
-          y0 += v[0] * xb.x + v[1] * xb.y + v[2] * xb.z;
-          y1 += v[3] * xb.x + v[4] * xb.y + v[5] * xb.z;
-          y2 += v[6] * xb.x + v[7] * xb.y + v[8] * xb.z;
+          y0 = fma(v[0], xb.x, y0);
+          y1 = fma(v[3], xb.x, y1);
+          y2 = fma(v[6], xb.x, y2);
+          y0 = fma(v[1], xb.y, y0);
+          y1 = fma(v[4], xb.y, y1);
+          y2 = fma(v[7], xb.y, y2);
+          y0 = fma(v[2], xb.z, y0);
+          y1 = fma(v[5], xb.z, y1);
+          y2 = fma(v[8], xb.z, y2);
         }
       }
 #pragma unroll

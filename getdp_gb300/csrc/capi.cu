@@ -729,6 +729,57 @@ int gb300_event_elapsed(gb300_ctx *ctx, int slot0, int slot1, float *ms)
   return GB300_OK;
 }
 
+// FP64 FMA throughput: eight independent dependency chains per thread, so
+// the FP64 pipe, not the FMA latency, limits the rate; the result is
+// consumed so that no chain is removed.
+__global__ void __launch_bounds__(256) k_fp64_fma(int iters, double a, double c,
+                                                  double *sink)
+{
+  double v[8];
+#pragma unroll
+  for(int k = 0; k < 8; k++) v[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+  for(int i = 0; i < iters; i++) {
+#pragma unroll
+    for(int k = 0; k < 8; k++) v[k] = fma(v[k], a, c);
+  }
+  double s = 0.;
+#pragma unroll
+  for(int k = 0; k < 8; k++) s += v[k];
+  if(s == 1234.5678) sink[0] = s;  // never true for these inputs; keeps the chains
+}
+
+int gb300_bench_fp64_peak(gb300_ctx *ctx, double *tflops)
+{
+  GB_TRY(check(ctx, "ctx"));
+  GB_TRY(check(tflops, "tflops"));
+  cudaStream_t st = ctx->stream;
+  int sms = 0, per_sm = 0;
+  GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fp64_fma, 256, 0));
+  const int grid = sms * (per_sm > 0 ? per_sm : 1);
+  const int iters = 4096;
+  DevBuf<double> sink;
+  GB_TRY(sink.alloc(1));
+  cudaEvent_t e0, e1;
+  GB_CUDA(cudaEventCreate(&e0));
+  GB_CUDA(cudaEventCreate(&e1));
+  k_fp64_fma<<<grid, 256, 0, st>>>(iters, 0.9999999, 1e-7, sink.p);  // warm-up
+  GB_CUDA(cudaEventRecord(e0, st));
+  const int reps = 5;
+  for(int r = 0; r < reps; r++)
+    k_fp64_fma<<<grid, 256, 0, st>>>(iters, 0.9999999, 1e-7, sink.p);
+  GB_CUDA(cudaEventRecord(e1, st));
+  GB_CUDA(cudaEventSynchronize(e1));
+  GB_CUDA(cudaGetLastError());
+  float ms = 0.f;
+  GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  double flops = 2.0 * 8.0 * iters * 256.0 * grid * reps;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return GB300_OK;
+}
+
 int gb300_bench_spmv(gb300_matrix *A, int precision, int reps, double *ms)
 {
   GB_TRY(check(A, "matrix"));

@@ -53,9 +53,8 @@ def term_arrays(p: Problem, dm: DofMap) -> dict:
     elif f == "curlcurl":
         kind = _lib.TERM_TET4_EDGE_CURLCURL
         a["elem_sign"] = np.ascontiguousarray(dm.elem_sign, np.int8)
-        a["source"] = np.ascontiguousarray(p.source, np.float64)
+        a["source"] = np.ascontiguousarray(p.source, np.float64).reshape(-1, 3)
         p0 = p.params["reg"]
-        p1 = p.params["J0"]
     else:
         raise ValueError(f)
     a["_kind"] = kind

@@ -273,15 +273,79 @@ def elasticity_p2(n: int, seed: int = 2, sigma_log: float = 0.5) -> Problem:
                     "g": 9.81})
 
 
+# Analytic potential of the toroidal source current: T = h(z) Psi(r) e_z about
+# the vertical axis through (0.5, 0.5), whose curl is the azimuthal current
+# J = -dPsi/dr h(z) e_phi = J0 beta((r - RC)/WR) beta((z - ZC)/WZ) e_phi with
+# the C2 bump beta(s) = (1 - s^2)^3 on |s| < 1: a coil of 1e6 A/m^2 peak in
+# 0.32 < r < 0.45, 0.3 < z < 0.7, around the iron cube.
+COIL_RC, COIL_WR, COIL_ZC, COIL_WZ = 0.385, 0.065, 0.5, 0.2
+
+
+def _bump_integral(s):
+    """int_{-1}^{s} (1 - t^2)^3 dt, clamped to [0, 32/35]."""
+    s = np.clip(s, -1.0, 1.0)
+    return s - s ** 3 + 0.6 * s ** 5 - s ** 7 / 7.0 + 16.0 / 35.0
+
+
+def toroidal_potential_z(P: np.ndarray, J0: float) -> np.ndarray:
+    """z component of T at points P (..., 3); T has no x, y components."""
+    r = np.hypot(P[..., 0] - 0.5, P[..., 1] - 0.5)
+    sz = np.clip((P[..., 2] - COIL_ZC) / COIL_WZ, -1.0, 1.0)
+    h = (1.0 - sz * sz) ** 3
+    return h * (-J0 * COIL_WR * _bump_integral((r - COIL_RC) / COIL_WR))
+
+
+def edge_circulation(a: np.ndarray, b: np.ndarray, J0: float, ng: int = 6) -> np.ndarray:
+    """int_a^b T . dl along straight edges (Gauss-Legendre, ng points)."""
+    t, w = np.polynomial.legendre.leggauss(ng)
+    t, w = 0.5 * (t + 1.0), 0.5 * w
+    d = b - a
+    acc = np.zeros(len(a))
+    for tk, wk in zip(t, w):
+        acc += wk * toroidal_potential_z(a + tk * d, J0)
+    return acc * d[:, 2]
+
+
+# the constant curls of the six Whitney functions of the reference tet
+# (BF_CurlEdge, src/functions/BF_Edge.cpp:452-485), local edge order of
+# GeoEntity.h:214-215
+_CURL_EDGE_REF = np.array([[0., -2., 2.], [2., 0., -2.], [-2., 2., 0.],
+                           [0., 0., 2.], [0., -2., 0.], [2., 0., 0.]])
+
+
+def curl_of_edge_interpolant(m: Mesh, J0: float) -> np.ndarray:
+    """Per element, the curl of the Whitney-edge interpolant of T: J_K =
+    sum_i t_i curl(w_i), t_i the circulation of T along edge i oriented from
+    the lower to the higher global node number.  The field is constant per
+    element and its normal component is continuous across faces, so it is
+    exactly divergence-free in the discrete sense: the right-hand side it
+    gives is orthogonal to every discrete gradient (to rounding), which the
+    nearly singular curl-curl operator (1e-6 mass regularisation) needs."""
+    x = m.nodes[m.elems]
+    c = np.stack([x[:, 1] - x[:, 0], x[:, 2] - x[:, 0], x[:, 3] - x[:, 0]], 1)
+    D = np.linalg.det(c)
+    J = np.zeros((m.n_elems, 3))
+    for i, (la, lb) in enumerate(TET4_EDGES):
+        na, nb = m.elems[:, la], m.elems[:, lb]
+        lo, hi = np.minimum(na, nb), np.maximum(na, nb)
+        t = edge_circulation(m.nodes[lo], m.nodes[hi], J0)
+        sg = np.where(na < nb, 1.0, -1.0)
+        cu = np.einsum("erc,er->ec", c, _CURL_EDGE_REF[i][None, :] * sg[:, None]) / D[:, None]
+        J += t[:, None] * cu
+    return J
+
+
 def curlcurl_edge(n: int, seed: int = 3) -> Problem:
     """3D magnetostatics with first-order Whitney edge elements (BF_Edge).
 
-    Iron cube [0.3,0.7]^3 with mu_r = 500 (by element centroid); a ring-coil
-    current of 1e6 A/m^2 circulating about the vertical axis through
-    (0.5, 0.5), in the annulus 0.32 < r < 0.45, 0.3 < z < 0.7 (coil elements
-    chosen by centroid, the azimuthal direction evaluated at each Gauss
-    point); regularisation 1e-6*nu*mass; n x a = 0 on the whole boundary.
-    Regions: 1 air, 2 iron, 3 coil.
+    Iron cube [0.3,0.7]^3 with mu_r = 500 (by element centroid); a toroidal
+    source current of 1e6 A/m^2 peak circulating about the vertical axis
+    through (0.5, 0.5) around the iron, given analytically as the curl of the
+    potential T (toroidal_potential_z) and taken per element as the curl of
+    T's edge interpolant (curl_of_edge_interpolant: divergence-free in the
+    discrete sense); regularisation 1e-6*nu*mass; n x a = 0 on the whole
+    boundary.  ``source`` is (n_elems, 3).  Regions: 1 air, 2 iron, 3
+    elements carrying current.
     """
     nodes, tets = _kuhn_tets(n)
     bt = _cube_boundary_tris(n)
@@ -289,14 +353,13 @@ def curlcurl_edge(n: int, seed: int = 3) -> Problem:
     reg = np.ones(len(tets), np.int32)
     iron = np.all((c > 0.3) & (c < 0.7), axis=1)
     reg[iron] = 2
-    r = np.hypot(c[:, 0] - 0.5, c[:, 1] - 0.5)
-    coil = (r > 0.32) & (r < 0.45) & (c[:, 2] > 0.3) & (c[:, 2] < 0.7)
-    reg[coil] = 3
     m = Mesh(nodes, TET4, tets, reg, "tri3", bt, np.full(len(bt), 30, np.int32))
+    J0 = 1.0e6
+    js = curl_of_edge_interpolant(m, J0)
+    reg[~iron & np.any(js != 0.0, axis=1)] = 3
     nu = np.where(reg == 2, 1.0 / (500.0 * MU0), 1.0 / MU0)
-    return Problem(f"curlcurl_edge_n{n}", m, "curlcurl", nu,
-                   (reg == 3).astype(np.float64),
-                   {"n": n, "seed": seed, "J0": 1.0e6, "reg": 1.0e-6})
+    return Problem(f"curlcurl_edge_n{n}", m, "curlcurl", nu, js,
+                   {"n": n, "seed": seed, "J0": J0, "reg": 1.0e-6})
 
 
 def eddy_2d(n: int, seed: int = 4, freq: Optional[float] = None,
@@ -704,17 +767,18 @@ Resolution {{ {{ Name R; System {{ {{ Name A; NameOfFormulation F; }} }}
   Operation {{ {_DUMP_OPS} }} }} }}
 """
     if f == "curlcurl":
-        J0 = p.params["J0"]
         rg = p.params["reg"]
+        ne = p.mesh.n_elems
+        lines = []
+        for k in range(ne):
+            lines.append(f"  nu[Region[{1000 + k}]] = {p.coef[k]:.17g};")
+            jx, jy, jz = p.source[k]
+            lines.append(f"  js[Region[{1000 + k}]] = Vector[{jx:.17g}, {jy:.17g}, {jz:.17g}];")
         return f"""Group {{
-  Air = Region[1]; Iron = Region[2]; Coil = Region[3];
-  Dom = Region[{{1,2,3}}]; Bnd = Region[30];
+  Dom = Region[{{{1000}:{1000 + ne - 1}}}]; Bnd = Region[30];
 }}
 Function {{
-  mu0 = {MU0:.17g};
-  nu[Iron] = 1./(500.*mu0);
-  nu[Region[{{1,3}}]] = 1./mu0;
-  js[Coil] = Vector[-(Y[]-0.5), X[]-0.5, 0] * ({J0:.17g} / Sqrt[(X[]-0.5)^2+(Y[]-0.5)^2]);
+{chr(10).join(lines)}
 }}
 Constraint {{ {{ Name a; Case {{ {{ Region Bnd; Value 0.; }} }} }} }}
 FunctionSpace {{
@@ -731,7 +795,7 @@ Formulation {{ {{ Name F; Type FemEquation;
   Equation {{
     Integral {{ [ nu[] * Dof{{d a}}, {{d a}} ]; In Dom; Jacobian Vol; Integration I1; }}
     Integral {{ [ {rg:.17g} * nu[] * Dof{{a}}, {{a}} ]; In Dom; Jacobian Vol; Integration I1; }}
-    Integral {{ [ -js[], {{a}} ]; In Coil; Jacobian Vol; Integration I1; }}
+    Integral {{ [ -js[], {{a}} ]; In Dom; Jacobian Vol; Integration I1; }}
   }} }} }}
 Resolution {{ {{ Name R; System {{ {{ Name A; NameOfFormulation F; }} }}
   Operation {{ {_DUMP_OPS} }} }} }}
@@ -766,9 +830,16 @@ PostOperation {{ {{ Name Map; NameOfPostProcessing P;
 """
 
 
-def write_pro(p: Problem, path: str) -> None:
-    """Write the problem file; elasticity needs one region per element."""
-    if p.formulation in ("elasticity", "nonlinear2d"):
+def prepare_regions(p: Problem) -> None:
+    """Formulations with per-element coefficients give every element its own
+    physical region (1000 + element index), as pro_text expects."""
+    if p.formulation in ("elasticity", "nonlinear2d", "curlcurl"):
         p.mesh.region = (1000 + np.arange(p.mesh.n_elems)).astype(np.int32)
+
+
+def write_pro(p: Problem, path: str) -> None:
+    """Write the problem file (after prepare_regions: write the mesh after
+    this call)."""
+    prepare_regions(p)
     with open(path, "w") as f:
         f.write(pro_text(p))

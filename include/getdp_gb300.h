@@ -188,7 +188,8 @@ int gb300_matrix_mult(gb300_matrix *A, const gb300_vector *x, gb300_vector *y);
 #define GB300_TERM_TET4_EDGE_CURLCURL 4
 /*   3D Whitney edges (BF_Edge) on 4-node tets, 4-point Gauss:
      [coef * Dof{d a}, {d a}] + [p0 * coef * Dof{a}, {a}] + [-js, {a}],
-     js = p1 * (-(y-0.5), x-0.5, 0) / r in elements with source != 0 */
+     js constant per element: source holds 3 values per element
+     (js_x, js_y, js_z; all zero = no source term) */
 #define GB300_TERM_TRI3_MAGNETOSTATIC_NL 5
 /*   2D a_z as TRI3_MAGNETOSTATIC with a field-dependent reluctivity, the
      Newton-Raphson terms of templates/Lib_Magnetostatics_a_phi.pro:186-193
@@ -206,7 +207,8 @@ typedef struct gb300_term_batch {
   const int *elem_dofs;          /* n_elems x local DOFs: unknown or -1 */
   const signed char *elem_sign;  /* n_elems x local DOFs (edges) or NULL */
   const double *coef;            /* per element */
-  const double *source;          /* per element, or NULL */
+  const double *source;          /* per element (3 per element for
+                                    TET4_EDGE_CURLCURL), or NULL */
   const double *coef2;           /* per element, or NULL */
   const double *coef3;           /* per element, or NULL: TRI3_EDDY_COMPLEX
                                     angular frequency (overrides p0), so one
@@ -273,6 +275,10 @@ int gb300_event_elapsed(gb300_ctx *ctx, int slot0, int slot1, float *ms);
    CG form q = A p with <p, q> fused; precision 0 FP64, 1 FP32 values and
    vectors) over `reps` launches timed with CUDA events after a warm-up. */
 int gb300_bench_spmv(gb300_matrix *A, int precision, int reps, double *ms);
+/* Measured FP64 FMA throughput of the context's device in TFLOP/s (two
+   flops per FMA): the denominator of the FP64-bound element kernels'
+   roofline. */
+int gb300_bench_fp64_peak(gb300_ctx *ctx, double *tflops);
 
 /* ---- residual without device allocation ------------------------------ */
 /* No counterpart in the reference: an entry point for callers that cannot

@@ -74,21 +74,36 @@ def _p(a, ct):
     return a.ctypes.data_as(ctypes.POINTER(ct))
 
 
-def assemble(problem, dofmap, ilu: str = "64", solution=None):
+def assemble(problem, dofmap, ilu: str = "64", solution=None, with_abs=False):
     """Run the restated element loop (at the current solution, for the
-    nonlinear formulation); returns (indptr, indices, data, b)."""
-    rr, cc, vv, b = assemble_coo(problem, dofmap, ilu, solution)
+    nonlinear formulation); returns (indptr, indices, data, b), plus with
+    with_abs the per-entry sums of |contribution| and the per-row sums of
+    |RHS contribution| (the rounding scales of sums in another order)."""
     L = lib(ilu)
+    babs = None
+    if with_abs:
+        babs = np.zeros(dofmap.n_dof, np.float64)
+        L.oracle_set_rhs_abs(_p(babs, ctypes.c_double))
+    try:
+        rr, cc, vv, b = assemble_coo(problem, dofmap, ilu, solution)
+    finally:
+        if with_abs:
+            L.oracle_set_rhs_abs(None)
     I32, D = ctypes.c_int32, ctypes.c_double
     n = dofmap.n_dof
     nz = len(vv)
     indptr = np.empty(n + 1, np.int32)
     indices = np.empty(max(nz, 1), np.int32)
     data = np.empty(max(nz, 1), np.float64)
+    absd = np.empty(max(nz, 1), np.float64) if with_abs else None
     nnz = L.oracle_coo_to_csr(n, ctypes.c_int64(nz), _p(rr, I32), _p(cc, I32),
                               _p(vv, D), _p(indptr, I32), _p(indices, I32),
-                              _p(data, D))
-    return indptr, indices[:nnz].copy(), data[:nnz].copy(), b
+                              _p(data, D), _p(absd, D) if with_abs else None)
+    del rr, cc, vv
+    out = (indptr, indices[:nnz].copy(), data[:nnz].copy(), b)
+    if with_abs:
+        return out + (absd[:nnz].copy(), babs)
+    return out
 
 
 def assemble_coo(problem, dofmap, ilu: str = "64", solution=None):
@@ -134,8 +149,8 @@ def assemble_coo(problem, dofmap, ilu: str = "64", solution=None):
             ne, _p(nodes, D), _p(elems, ctypes.c_int), _p(edofs, ctypes.c_int),
             _p(sg, ctypes.c_byte),
             _p(np.ascontiguousarray(problem.coef, np.float64), D),
-            _p(np.ascontiguousarray(problem.source, np.float64), D),
-            ctypes.c_double(problem.params["reg"]), ctypes.c_double(problem.params["J0"]),
+            _p(np.ascontiguousarray(problem.source, np.float64).reshape(ne, 3), D),
+            ctypes.c_double(problem.params["reg"]),
             ctypes.c_int64(cap), _p(rr, I32), _p(cc, I32), _p(vv, D), _p(b, D))
     elif f == "nonlinear2d":
         x = np.zeros(n) if solution is None else np.ascontiguousarray(solution, np.float64)

@@ -50,6 +50,16 @@ typedef struct {
   double c11, c12, c13, c21, c22, c23, c31, c32, c33;
 } M3;
 
+/* RHS accumulation; with g_babs set, also the sum of |contribution| per row
+   (the rounding scale of the same sum taken in another order) */
+static double *g_babs = NULL;
+void oracle_set_rhs_abs(double *babs) { g_babs = babs; }
+static void badd(double *b, int row, double v)
+{
+  b[row] += v;
+  if(g_babs) g_babs[row] += fabs(v);
+}
+
 /* COO sink in call order */
 typedef struct {
   int64_t n, cap;
@@ -285,12 +295,12 @@ int64_t oracle_assemble_tri3_nl(int ne, const double *nodes, const int *elems,
       }
     }
     for(i = 0; i < 3; i++)
-      if(dof[i] >= 0 && Eb1[i]) b[dof[i]] += (1. * 1.) * -Eb1[i];
+      if(dof[i] >= 0 && Eb1[i]) badd(b, dof[i], (1. * 1.) * -Eb1[i]);
     for(i = 0; i < 3; i++)
       for(j = 0; j < 3; j++)
         if(dof[i] >= 0 && dof[j] >= 0) coo_add(&m, dof[i], dof[j], Ek[i][j]);
     for(i = 0; i < 3; i++)
-      if(dof[i] >= 0 && Eb3[i]) b[dof[i]] += (1. * 1.) * -Eb3[i];
+      if(dof[i] >= 0 && Eb3[i]) badd(b, dof[i], (1. * 1.) * -Eb3[i]);
     if(js[e] != 0.) {
       double Es[3] = {0., 0., 0.};
       for(q = 0; q < 3; q++) {
@@ -300,7 +310,7 @@ int64_t oracle_assemble_tri3_nl(int ne, const double *nodes, const int *elems,
       }
       for(i = 0; i < 3; i++) {
         if(dof[i] < 0 || !Es[i]) continue;
-        b[dof[i]] += (1. * 1.) * -Es[i];
+        badd(b, dof[i], (1. * 1.) * -Es[i]);
       }
     }
   }
@@ -384,7 +394,7 @@ int64_t oracle_assemble_tri_p1(int ne, const double *nodes, const int *elems,
       }
       for(i = 0; i < 3; i++) {
         if(dof[i] < 0 || !Eb[i]) continue;
-        b[dof[i]] += (1. * 1.) * -Eb[i];
+        badd(b, dof[i], (1. * 1.) * -Eb[i]);
       }
     }
   }
@@ -486,7 +496,7 @@ int64_t oracle_assemble_tet10_elasticity(int ne, const double *nodes,
       for(i = 0; i < 10; i++) {
         int r = dof[20 + i];
         if(r < 0 || !Eb[i]) continue;
-        b[r] += (1. * 1.) * -Eb[i];
+        badd(b, r, (1. * 1.) * -Eb[i]);
       }
     }
   }
@@ -522,8 +532,8 @@ static void curl_edge_tet(int k, double s[3])
 int64_t oracle_assemble_tet4_curlcurl(int ne, const double *nodes,
                                       const int *elems, const int *edofs,
                                       const signed char *esign,
-                                      const double *nu, const double *coil,
-                                      double reg, double J0, int64_t cap,
+                                      const double *nu, const double *js,
+                                      double reg, int64_t cap,
                                       int32_t *rr, int32_t *cc, double *vv,
                                       double *b)
 {
@@ -590,23 +600,18 @@ int64_t oracle_assemble_tet4_curlcurl(int ne, const double *nodes,
     for(i = 0; i < 6; i++)
       for(j = 0; j < 6; j++)
         if(dof[i] >= 0 && dof[j] >= 0) coo_add(&m, dof[i], dof[j], Ek[i][j]);
-    /* term 3: ring-coil source */
-    if(coil[e] != 0.) {
+    /* term 3: [ -js[], {a} ] with js[] a constant vector per element
+       (the curl of the edge interpolant of an analytic potential) */
+    if(js[3 * e] != 0. || js[3 * e + 1] != 0. || js[3 * e + 2] != 0.) {
       double Eb[6] = {0., 0., 0., 0., 0., 0.};
+      double jv[3];
+      jv[0] = -js[3 * e];
+      jv[1] = -js[3 * e + 1];
+      jv[2] = -js[3 * e + 2];
       for(q = 0; q < 4; q++) {
-        double u = XTET4[q], v = YTET4[q], w = ZTET4[q];
-        double n4[4] = {1. - u - v - w, u, v, w};
-        double X = 0., Y = 0., dx, dy, s, jv[3], F;
-        for(i = 0; i < 4; i++) X += x[i] * n4[i];
-        for(i = 0; i < 4; i++) Y += y[i] * n4[i];
+        double u = XTET4[q], v = YTET4[q], w = ZTET4[q], F;
         D = jac3d(4, x, y, z, g, &J);
         inv3d(D, &J, &I);
-        dx = X - 0.5;
-        dy = Y - 0.5;
-        s = J0 / sqrt(dx * dx + dy * dy);
-        jv[0] = -(-dy * s);
-        jv[1] = -(dx * s);
-        jv[2] = -(0. * s);
         F = 1. * (PTET4[q] * fabs(D));
         for(i = 0; i < 6; i++) {
           double sv[3], xv[3];
@@ -618,7 +623,7 @@ int64_t oracle_assemble_tet4_curlcurl(int ne, const double *nodes,
       }
       for(i = 0; i < 6; i++) {
         if(dof[i] < 0 || !Eb[i]) continue;
-        b[dof[i]] += (1. * 1.) * -Eb[i];
+        badd(b, dof[i], (1. * 1.) * -Eb[i]);
       }
     }
   }
@@ -631,8 +636,11 @@ int64_t oracle_assemble_tet4_curlcurl(int ne, const double *nodes,
 /* ---------------------------------------------------------------------- */
 int64_t oracle_coo_to_csr(int n, int64_t nz, const int32_t *r, const int32_t *c,
                           const double *v, int32_t *indptr, int32_t *indices,
-                          double *data)
+                          double *data, double *absdata)
 {
+  /* absdata (may be NULL): per entry, the sum of the absolute values of the
+     contributions merged into it -- the scale of the rounding error of a
+     sum taken in another order */
   int64_t *cnt = (int64_t *)calloc((size_t)n + 1, sizeof(int64_t));
   int64_t *p1 = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nz ? nz : 1));
   int64_t *p2 = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nz ? nz : 1));
@@ -654,11 +662,13 @@ int64_t oracle_coo_to_csr(int n, int64_t nz, const int32_t *r, const int32_t *c,
     int64_t s = p2[k];
     if(out > 0 && r[s] == r[p2[k - 1]] && c[s] == indices[out - 1]) {
       data[out - 1] += v[s];
+      if(absdata) absdata[out - 1] += fabs(v[s]);
       continue;
     }
     while(i < r[s]) indptr[++i] = (int32_t)out;
     indices[out] = c[s];
     data[out] = v[s];
+    if(absdata) absdata[out] = fabs(v[s]);
     out++;
   }
   while(i < n) indptr[++i] = (int32_t)out;

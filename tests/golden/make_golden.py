@@ -16,7 +16,7 @@ seeded instances of every workload, and stores for each:
 
 This script needs the reference sources and only runs in the development
 container; the fixtures it writes are committed and travel with the tests.
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [case names...]   (default: all)
 """
 from __future__ import annotations
 
@@ -161,13 +161,18 @@ def run_case(name, gen, kw, par, exe="getdp_ilu64"):
 def main():
     if not os.path.exists(os.path.join(REF_BIN, "getdp_ilu64")):
         raise SystemExit("build the reference first: oracle/build_ref.sh")
+    only = set(sys.argv[1:])
     for name, gen, kw, par in CASES:
+        if only and name not in only:
+            continue
         d = run_case(name, gen, kw, par)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **d)
         print(f"{name}: n={d['n']} nnz={len(d['data'])} its={d['iterations']} "
               f"res={d['residual']:.3e}")
     # the FP32-ILU flavour (the official build's HAVE_ILU_FLOAT) on one case
     name, gen, kw, par = CASES[1]
+    if only and name + "_ilu32" not in only:
+        return
     d = run_case(name + "_ilu32", gen, kw, par, exe="getdp_ilu32")
     np.savez_compressed(os.path.join(HERE, f"{name}_ilu32.npz"), **d)
     print(f"{name}_ilu32: its={d['iterations']} res={d['residual']:.3e}")

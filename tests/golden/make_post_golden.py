@@ -61,6 +61,7 @@ def run(name, gen, kw, dim):
     if dim == 2:
         pts[:, 2] = 0.0
     tmp = tempfile.mkdtemp(prefix="postgolden_")
+    W.prepare_regions(p)
     try:
         with open(os.path.join(tmp, "p.pro"), "w") as f:
             f.write(W.pro_text(p) + W.post_text(p, [tuple(q) for q in pts]))
@@ -93,7 +94,10 @@ def run(name, gen, kw, dim):
 
 
 def main():
+    only = set(sys.argv[1:])
     for name, gen, kw, dim in CASES:
+        if only and name not in only:
+            continue
         d = run(name, gen, kw, dim)
         d["gen_kw_keys"] = np.array(list(kw.keys()))
         d["gen_kw_vals"] = np.array([float(v) for v in kw.values()])

@@ -2,8 +2,9 @@
 
 Tolerances (FP64):
 * CSR pattern: identical to the reference's (bit-exact integers);
-* matrix and RHS values: |gpu - ref| <= 1e-12 * |ref| + 1e-14 * max|row of ref|
-  (summation order differs: atomics, fused multiply-adds);
+* matrix and RHS values: |gpu - ref| <= 1e-12 |ref| + 1e-13 S, S the
+  entry's rounding scale sqrt(A_ii A_jj) (tests/tolerances.py: the summation
+  order differs -- atomics, fused multiply-adds);
 * the LinAlg add path (entries added one by one in the reference's call
   order): bit-exact;
 * solutions: converged (status 0); with the reference's own tolerance the
@@ -18,19 +19,20 @@ from getdp_gb300 import generate as G_
 from getdp_gb300 import linalg as LA
 from getdp_gb300 import workloads as W
 from tests import golden_cases as G
+from tests import tolerances as TOL
 
 pytestmark = pytest.mark.gpu
 
 ASSEMBLY_CASES = [n for n in G.names() if not n.endswith("ilu32")]
 
 
-def close_values(got, ref, indptr):
-    rowmax = np.zeros(len(ref))
-    for i in range(len(indptr) - 1):
-        s, e = indptr[i], indptr[i + 1]
-        if e > s:
-            rowmax[s:e] = np.max(np.abs(ref[s:e]))
-    return np.all(np.abs(got - ref) <= 1e-12 * np.abs(ref) + 1e-14 * rowmax)
+def _abs_sums(p, dm, indptr, indices, data, solution=None):
+    """The rounding scales of tests/tolerances.py for the reference matrix
+    (indptr, indices, data): per entry and per RHS row (the oracle's pattern
+    is the reference's: checked)."""
+    oip, oix, _, _, sabs, babs = oracle.assemble(p, dm, solution=solution, with_abs=True)
+    assert np.array_equal(oip, indptr) and np.array_equal(oix, indices)
+    return TOL.matrix_scale(indptr, indices, data, sabs, p.formulation == "eddy2d"), babs
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -47,10 +49,10 @@ def test_generate_matches_reference(name):
     ip, ix, dv = A.csr()
     assert np.array_equal(ip, d["indptr"])
     assert np.array_equal(ix, d["indices"])
-    assert close_values(dv, d["data"], d["indptr"])
+    sabs, babs = _abs_sums(p, dm, d["indptr"], d["indices"], d["data"])
+    assert TOL.values_close(dv, d["data"], sabs), TOL.report(dv, d["data"], sabs)
     bb = b.numpy()
-    assert np.all(np.abs(bb - d["b"]) <= 1e-12 * np.abs(d["b"]) +
-                  1e-14 * np.max(np.abs(d["b"])))
+    assert TOL.values_close(bb, d["b"], babs), TOL.report(bb, d["b"], babs)
 
 
 @pytest.mark.parametrize("name", ASSEMBLY_CASES)
@@ -71,7 +73,8 @@ def test_linalg_add_path_bit_exact(name):
         f"{np.max(np.abs(dv - odv) / np.maximum(np.abs(odv), 1e-300)):.2e}")
     # and the reference's values (an element value computed on another
     # architecture can differ in its last bit)
-    assert close_values(dv, d["data"], d["indptr"])
+    sabs, _ = _abs_sums(p, dm, d["indptr"], d["indices"], d["data"])
+    assert TOL.values_close(dv, d["data"], sabs)
 
 
 def _solver(params: dict):

@@ -3,8 +3,8 @@ loop of the reference's nonlinear resolution, against fixtures of the
 reference itself (tests/golden/newton_*.npz, make_nl_golden.py) and the
 oracle.
 
-Tolerances: matrix and RHS of a Generate within 1e-12 relative (plus 1e-14
-of the row maximum); the residual history within 1e-9 of res0 plus 1e-6 of
+Tolerances: matrix and RHS of a Generate within 1e-12 relative plus 1e-13
+of the entry's rounding scale (tests/tolerances.py); the residual history within 1e-9 of res0 plus 1e-6 of
 each value (the linear solves stop at 1e-13, so iterates differ by that
 much, amplified by the problem's conditioning); the same number of Newton
 steps; final solutions within 1e-7 relative.
@@ -16,6 +16,7 @@ import pytest
 
 import oracle
 from getdp_gb300 import workloads as W
+from tests import tolerances as TOL
 from tests.golden_cases import GOLDEN
 
 NAMES = ["newton_nl2d_n12", "newton_nl2d_n16"]
@@ -39,12 +40,6 @@ def solve_kw(d):
                 renumbering=int(par["Renumbering_Technique"]))
 
 
-def close_values(got, ref, indptr):
-    rowmax = np.repeat([np.max(np.abs(ref[indptr[i]:indptr[i + 1]]))
-                        for i in range(len(indptr) - 1)], np.diff(indptr))
-    return np.all(np.abs(got - ref) <= 1e-12 * np.abs(ref) + 1e-14 * rowmax)
-
-
 def close_history(h, ref):
     return len(h) == len(ref) and np.all(np.abs(np.asarray(h) - ref) <=
                                          1e-9 * ref[0] + 1e-6 * np.abs(ref))
@@ -53,10 +48,12 @@ def close_history(h, ref):
 @pytest.mark.parametrize("name", NAMES)
 def test_oracle_first_generate_matches_reference(name):
     d, p, dm = load(name)
-    ip, ix, dv, b = oracle.assemble(p, dm)
+    ip, ix, dv, b, sabs, babs = oracle.assemble(p, dm, with_abs=True)
     assert np.array_equal(ip, d["indptr"]) and np.array_equal(ix, d["indices"])
-    assert close_values(dv, d["data"], d["indptr"])
-    assert np.all(np.abs(b - d["b"]) <= 1e-12 * np.abs(d["b"]) + 1e-14 * np.abs(d["b"]).max())
+    # exp() of the host's libm against the reference's build: last bits
+    sabs = TOL.matrix_scale(ip, ix, dv, sabs)
+    assert TOL.values_close(dv, d["data"], sabs)
+    assert TOL.values_close(b, d["b"], babs)
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -88,17 +85,20 @@ def test_gpu_generate_matches_reference_and_oracle(name):
     G_.generate(A, b, terms.batch, pattern=True, solution=x)  # x = 0
     ip, ix, dv = A.csr()
     assert np.array_equal(ip, d["indptr"]) and np.array_equal(ix, d["indices"])
-    assert close_values(dv, d["data"], d["indptr"])
+    _, _, _, _, sabs, babs = oracle.assemble(p, dm, with_abs=True)
+    sabs = TOL.matrix_scale(d["indptr"], d["indices"], d["data"], sabs)
+    assert TOL.values_close(dv, d["data"], sabs)
     bb = b.numpy()
-    assert np.all(np.abs(bb - d["b"]) <= 1e-12 * np.abs(d["b"]) + 1e-14 * np.abs(d["b"]).max())
+    assert TOL.values_close(bb, d["b"], babs)
     # at a field deep in the nonlinear range: the reference's final solution
     x.set(d["x"])
     G_.generate(A, b, terms.batch, pattern=False, solution=x)
-    oip, oix, odv, ob = oracle.assemble(p, dm, solution=d["x"])
+    oip, oix, odv, ob, sabs, babs = oracle.assemble(p, dm, solution=d["x"], with_abs=True)
     ip, ix, dv = A.csr()
-    assert np.array_equal(ip, oip) and close_values(dv, odv, oip)
+    sabs = TOL.matrix_scale(oip, oix, odv, sabs)
+    assert np.array_equal(ip, oip) and TOL.values_close(dv, odv, sabs)
     bb = b.numpy()
-    assert np.all(np.abs(bb - ob) <= 1e-12 * np.abs(ob) + 1e-14 * np.abs(ob).max())
+    assert TOL.values_close(bb, ob, babs)
 
 
 @pytest.mark.gpu
