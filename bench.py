@@ -200,6 +200,28 @@ class Clocks:
         return out
 
 
+# FP64 operations per element of the P2 elasticity element kernel, counted by
+# ncu on the GPU (2 DFMA + DADD + DMUL thread instructions, active lanes only;
+# profiles/tet10_elasticity_values_n32.md); bytes per element as the
+# algorithmic minimum (connectivity 40 B, coordinates 33 B, coefficient 4 B,
+# the CSR values written once 8 nnz / E, the RHS 8 N / E)
+TET10_FP64_FLOPS_PER_ELEMENT = 10970
+
+
+def assembly_roofline(ne, n, nnz, t, fp64_tflops, hbm_gbs):
+    """Generate (cached pattern: table comparison, zeroing, element kernel)
+    against the FP64 pipe (measured FMA peak) and HBM (measured copy)."""
+    flops = TET10_FP64_FLOPS_PER_ELEMENT * ne
+    bytes_ = ne * (40 + 4) + (n // 3) * 24 + 8 * nnz + 8 * n
+    ach = flops / t / 1e12
+    gbs = bytes_ / t / 1e9
+    return {"bound": "fp64", "unit": "TFLOP/s", "achieved": ach, "peak": fp64_tflops,
+            "frac": ach / fp64_tflops, "peak_kind": "measured (gb300_bench_fp64_peak)",
+            "flops_per_element": TET10_FP64_FLOPS_PER_ELEMENT,
+            "algorithmic_bytes": bytes_, "achieved_gbs": gbs, "hbm_frac": gbs / hbm_gbs,
+            "generate_s": t, "elements": ne}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -605,10 +627,11 @@ def run_nonlinear(args, ws, rank, local):
         S["stopping_test"] = 1e-10
         return S
 
-    def run_gpu(size, prec, reps):
+    def run_gpu(size, prec, reps, scatter=_lib.SCATTER_DEFAULT):
         p = W.nonlinear_2d(n=size, seed=5)
         dm = W.dofmap_for(p)
         terms = G.DeviceTerms(p, dm)
+        terms.batch.scatter = scatter
         out = None
         ts = []
         for _ in range(reps):
@@ -627,6 +650,16 @@ def run_nonlinear(args, ws, rank, local):
         run_gpu(n, prec, 1)  # warm-up (pattern, colouring, tuning)
         res[prec], _ = run_gpu(n, prec, max(args.steps, 1))
     best = min(res.values(), key=lambda r: r["s"])
+    # the same with the coloured (atomic-free) scatter: Generate, and so the
+    # whole Newton loop, gives the same numbers on every run
+    det = []
+    for _ in range(2):
+        r, o = run_gpu(n, 1, 1, scatter=_lib.SCATTER_COLOURED)
+        det.append((r, float(o.history[-1])))
+    deterministic = dict(det[1][0])
+    deterministic["repeat_identical"] = bool(
+        det[0][0]["linear_iterations"] == det[1][0]["linear_iterations"] and
+        det[0][1] == det[1][1])
     learned = None
     if args.learned_weights:
         from getdp_gb300 import learned as LR
@@ -655,7 +688,7 @@ def run_nonlinear(args, ws, rank, local):
                                    "Newton, ILU(0)-(F)GMRES(50) per step",
                        "elements": 2 * n * n, "unknowns": res[0]["unknowns"],
                        "parallelism": f"replicas x{ws}"},
-            "fp64": res[0], "mixed": res[1]}
+            "fp64": res[0], "mixed": res[1], "mixed_coloured_scatter": deterministic}
     if learned is not None:
         line["learned_mixed"] = learned
     if not args.skip_cpu and rank == 0:
@@ -750,14 +783,32 @@ def main():
         _lib.check(L.gb300_event_elapsed(ctx, a, c, ctypes.byref(ms)))
         return ms.value / 1e3
 
-    # components, once (outside the timed region)
+    # components, once (outside the timed region): the first Generate builds
+    # the pattern and caches it on the context; a Generate of the same
+    # element table reuses it (the steady state of every step)
     ev(0)
     G.generate(A, b, terms.batch, pattern=True)
     ev(1)
-    G.generate(A, b, terms.batch, pattern=False)
+    G.generate(A, b, terms.batch, pattern=True)
     ev(2)
-    t_gen_full, t_gen_values = elapsed(0, 1), elapsed(1, 2)
+    t_gen_cold, t_gen_full = elapsed(0, 1), elapsed(1, 2)
+    t_gen_values = t_gen_full
     nnz = A.nnz()
+    # the scatter modes of the element kernel, each timed warm (its first
+    # call builds the position table or the colouring, once per pattern)
+    scatter_modes = {}
+    for name, m in (("search_atomic", _lib.SCATTER_SEARCH), ("table_atomic", _lib.SCATTER_TABLE),
+                    ("coloured_no_atomics", _lib.SCATTER_COLOURED)):
+        ev(0)
+        G.generate(A, b, terms.batch, pattern=True, scatter=m)
+        ev(1)
+        G.generate(A, b, terms.batch, pattern=True, scatter=m)
+        ev(2)
+        scatter_modes[name] = {"first_s": elapsed(0, 1), "s": elapsed(1, 2)}
+    terms.batch.scatter = _lib.SCATTER_DEFAULT
+    fp64_peak = ctypes.c_double()
+    _lib.check(L.gb300_bench_fp64_peak(ctx, ctypes.byref(fp64_peak)))
+    fp64_peak = fp64_peak.value
     if args.no_plain:
         info_plain, t_plain = {"iterations": None}, None
     else:
@@ -890,8 +941,11 @@ def main():
                    "elements": p.mesh.n_elems, "unknowns": N, "nnz": nnz,
                    "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2, no flush"},
         "assembly_gdof_s": N / t_gen_full / 1e9,
-        "assembly_values_only_gdof_s": N / t_gen_values / 1e9,
-        "generate_s": t_gen_full, "generate_values_only_s": t_gen_values,
+        "assembly_cold_gdof_s": N / t_gen_cold / 1e9,
+        "generate_s": t_gen_full, "generate_cold_s": t_gen_cold,
+        "generate_scatter_modes": scatter_modes,
+        "roofline_assembly": assembly_roofline(p.mesh.n_elems, N, nnz, t_gen_full,
+                                               fp64_peak, peak),
         "solve_iterations": inf["iterations"], "reliable_updates": inf["refinement_steps"],
         "true_rel_residual": inf["true_residual"] / inf["rhs_norm"],
         "plain_fp64_solve_s": t_plain, "plain_fp64_iterations": info_plain["iterations"],

@@ -53,7 +53,7 @@ class SolveInfo(ctypes.Structure):
                 ("residual_estimate", ctypes.c_double),
                 ("true_residual", ctypes.c_double), ("rhs_norm", ctypes.c_double),
                 ("refinement_steps", ctypes.c_int),
-                ("inner_iterations", ctypes.c_int)]
+                ("inner_iterations", ctypes.c_int), ("ilu_factorized", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -66,7 +66,13 @@ class TermBatch(ctypes.Structure):
                 ("elem_sign", ctypes.c_void_p), ("coef", ctypes.c_void_p),
                 ("source", ctypes.c_void_p), ("coef2", ctypes.c_void_p),
                 ("coef3", ctypes.c_void_p), ("p0", ctypes.c_double), ("p1", ctypes.c_double),
-                ("p2", ctypes.c_double), ("on_device", ctypes.c_int)]
+                ("p2", ctypes.c_double), ("on_device", ctypes.c_int),
+                ("fixed_values", ctypes.c_void_p), ("n_fixed", ctypes.c_int),
+                ("scatter", ctypes.c_int)]
+
+
+# gb300_term_batch.scatter
+SCATTER_DEFAULT, SCATTER_SEARCH, SCATTER_TABLE, SCATTER_COLOURED = 0, 1, 2, 3
 
 
 # every symbol of include/getdp_gb300.h with (restype, argtypes)
@@ -139,6 +145,7 @@ SIGNATURES = {
     "gb300_event_elapsed": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_float)]),
     "gb300_bench_spmv": (_I, [_P, _I, _I, ctypes.POINTER(_D)]),
     "gb300_bench_fp64_peak": (_I, [_P, ctypes.POINTER(_D)]),
+    "gb300_bench_dmma_peak": (_I, [_P, ctypes.POINTER(_D)]),
     "gb300_residual_noalloc": (_I, [_P, _P, _P, _P, ctypes.POINTER(_D)]),
 }
 

@@ -179,19 +179,32 @@ __device__ __forceinline__ void bsr_block(const int *__restrict__ col,
 {
   int b = mload<CS>(col + k);
   auto xb = Vec4<T>::load(p + 4 * (size_t)b);
-  // nine chained FMAs per block: `y += a x + b y + c z` compiles to a
-  // multiply, two FMAs and an add per row (12 FP64 instructions per block
-  // instead of 9), and GB300's FP64 pipe (2 FMAs per SM per cycle) bounds
-  // the FP64 product
-  y0 = fma(mload<CS>(val + k), xb.x, y0);
-  y1 = fma(mload<CS>(val + 3 * nblk + k), xb.x, y1);
-  y2 = fma(mload<CS>(val + 6 * nblk + k), xb.x, y2);
-  y0 = fma(mload<CS>(val + nblk + k), xb.y, y0);
-  y1 = fma(mload<CS>(val + 4 * nblk + k), xb.y, y1);
-  y2 = fma(mload<CS>(val + 7 * nblk + k), xb.y, y2);
-  y0 = fma(mload<CS>(val + 2 * nblk + k), xb.z, y0);
-  y1 = fma(mload<CS>(val + 5 * nblk + k), xb.z, y1);
-  y2 = fma(mload<CS>(val + 8 * nblk + k), xb.z, y2);
+  if constexpr(sizeof(T) == 8) {
+    // FP64: nine chained FMAs per block.  `y += a x + b y + c z` compiles to
+    // a multiply, two FMAs and an add per row (12 FP64 instructions per
+    // block instead of 9), and GB300's FP64 pipe (2 FMAs per SM per cycle)
+    // bounds the FP64 product
+    y0 = fma(mload<CS>(val + k), xb.x, y0);
+    y1 = fma(mload<CS>(val + 3 * nblk + k), xb.x, y1);
+    y2 = fma(mload<CS>(val + 6 * nblk + k), xb.x, y2);
+    y0 = fma(mload<CS>(val + nblk + k), xb.y, y0);
+    y1 = fma(mload<CS>(val + 4 * nblk + k), xb.y, y1);
+    y2 = fma(mload<CS>(val + 7 * nblk + k), xb.y, y2);
+    y0 = fma(mload<CS>(val + 2 * nblk + k), xb.z, y0);
+    y1 = fma(mload<CS>(val + 5 * nblk + k), xb.z, y1);
+    y2 = fma(mload<CS>(val + 8 * nblk + k), xb.z, y2);
+  }
+  else {
+    // FP32 (memory bound): each row's three products first, then one add
+    // (measured faster than the chained form: 0.2036 against 0.2096 ms per
+    // launch at 48^3)
+    y0 += mload<CS>(val + k) * xb.x + mload<CS>(val + nblk + k) * xb.y +
+          mload<CS>(val + 2 * nblk + k) * xb.z;
+    y1 += mload<CS>(val + 3 * nblk + k) * xb.x + mload<CS>(val + 4 * nblk + k) * xb.y +
+          mload<CS>(val + 5 * nblk + k) * xb.z;
+    y2 += mload<CS>(val + 6 * nblk + k) * xb.x + mload<CS>(val + 7 * nblk + k) * xb.y +
+          mload<CS>(val + 8 * nblk + k) * xb.z;
+  }
 }
 
 // MINB: CTAs per SM the register allocation must allow (0 = the compiler's

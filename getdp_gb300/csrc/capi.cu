@@ -93,6 +93,8 @@ int gb300_ctx_destroy(gb300_ctx *ctx)
 {
   if(!ctx) return GB300_OK;
   cudaStreamSynchronize(ctx->stream);
+  gb::gen_cache_free(ctx->gen);
+  ctx->gen = nullptr;
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return GB300_OK;
@@ -672,10 +674,12 @@ int gb300_generate_pattern(gb300_matrix *A, const gb300_term_batch *t)
 {
   GB_TRY(check(A, "matrix"));
   GB_TRY(check(t, "term batch"));
+  // a Generate makes a new matrix (GetDP's ZeroMatrix): no factor survives it
   if(A->ilu) {
     ilu_free(A->ilu);
     A->ilu = nullptr;
   }
+  colour_drop_factor(A);
   return generate_pattern(A, t);
 }
 
@@ -776,6 +780,61 @@ int gb300_bench_fp64_peak(gb300_ctx *ctx, double *tflops)
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   double flops = 2.0 * 8.0 * iters * 256.0 * grid * reps;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return GB300_OK;
+}
+
+// FP64 tensor-core (DMMA) throughput: each warp keeps four independent
+// m8n8k4 accumulators (D = A B + D, 512 flops per warp instruction)
+__global__ void __launch_bounds__(256) k_fp64_dmma(int iters, double *sink)
+{
+  const int lane = threadIdx.x & 31;
+  double a = 1.0 + 1e-3 * lane, b = 1.0 - 1e-3 * lane;
+  double acc[4][2];
+#pragma unroll
+  for(int k = 0; k < 4; k++) acc[k][0] = acc[k][1] = 0.;
+  for(int i = 0; i < iters; i++) {
+#pragma unroll
+    for(int k = 0; k < 4; k++)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 "
+                   "{%0, %1}, {%2}, {%3}, {%0, %1};"
+                   : "+d"(acc[k][0]), "+d"(acc[k][1])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.;
+#pragma unroll
+  for(int k = 0; k < 4; k++) s += acc[k][0] + acc[k][1];
+  if(s == 1234.5678) sink[0] = s;  // never true for these inputs
+}
+
+int gb300_bench_dmma_peak(gb300_ctx *ctx, double *tflops)
+{
+  GB_TRY(check(ctx, "ctx"));
+  GB_TRY(check(tflops, "tflops"));
+  cudaStream_t st = ctx->stream;
+  int sms = 0, per_sm = 0;
+  GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fp64_dmma, 256, 0));
+  const int grid = sms * (per_sm > 0 ? per_sm : 1);
+  const int iters = 1024;
+  DevBuf<double> sink;
+  GB_TRY(sink.alloc(1));
+  cudaEvent_t e0, e1;
+  GB_CUDA(cudaEventCreate(&e0));
+  GB_CUDA(cudaEventCreate(&e1));
+  k_fp64_dmma<<<grid, 256, 0, st>>>(iters, sink.p);  // warm-up
+  GB_CUDA(cudaEventRecord(e0, st));
+  const int reps = 5;
+  for(int r = 0; r < reps; r++) k_fp64_dmma<<<grid, 256, 0, st>>>(iters, sink.p);
+  GB_CUDA(cudaEventRecord(e1, st));
+  GB_CUDA(cudaEventSynchronize(e1));
+  GB_CUDA(cudaGetLastError());
+  float ms = 0.f;
+  GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const double warps = grid * 256.0 / 32.0;
+  const double flops = 512.0 * 4.0 * iters * warps * reps;
   *tflops = flops / (ms * 1e-3) / 1e12;
   return GB300_OK;
 }

@@ -217,6 +217,14 @@ __global__ void k_scatter_rows(int n, const int *__restrict__ old_of,
   if(i < n) out[old_of[i]] = in[i];
 }
 
+void colour_drop_factor(gb300_matrix *A)
+{
+  if(A->mc && A->mc->B && A->mc->B->ilu) {
+    ilu_free(A->mc->B->ilu);
+    A->mc->B->ilu = nullptr;
+  }
+}
+
 void colour_free(Colouring *c)
 {
   if(!c) return;

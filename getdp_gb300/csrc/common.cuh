@@ -258,11 +258,20 @@ template <typename K> int resident_grid(K kernel, int threads, size_t smem)
 
 }  // namespace gb
 
+namespace gb {
+struct GenCache;  // the pattern of the last Generate (assemble.cu)
+void gen_cache_free(GenCache *c);
+}  // namespace gb
+
 // the objects behind the opaque handles of the C ABI
 struct gb300_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int num_sms = 152;
+  // CSR pattern, scatter positions and element colouring of the element
+  // table last generated on this context: a Generate of the same table
+  // (GetDP's ZeroMatrix recreates A before every Generate) reuses them
+  gb::GenCache *gen = nullptr;
 };
 
 struct gb300_vector {
@@ -304,4 +313,8 @@ struct gb300_matrix {
   // corr_version == pattern_version)
   gb::DevBuf<double> corr;
   unsigned corr_version = ~0u;
+  // the pattern came from the context's Generate cache entry gen_tag while
+  // pattern_version was gen_pv (a later change of the pattern bumps the
+  // version and so invalidates the link)
+  unsigned gen_tag = 0, gen_pv = ~0u;
 };

@@ -63,7 +63,8 @@ struct ilu_data {
   std::vector<Segment> lseg, useg;
   DevBuf<double> lu64, inv64;
   DevBuf<float> lu32, inv32;
-  bool fact64 = false, fact32 = false;
+  bool fact64 = false, fact32 = false;  // a factor of that precision is held
+  unsigned version = ~0u;               // the matrix pattern it was set up for
 };
 
 void ilu_free(ilu_data *d) { delete d; }
@@ -288,11 +289,13 @@ static int ell_values(EllPart &E, const T *lu, DevBuf<T> &v, cudaStream_t st)
 
 static int ilu_setup(gb300_matrix *A)
 {
-  if(A->ilu && A->ilu->n == A->n) return GB300_OK;
+  // the level schedule and diagonal positions belong to one pattern
+  if(A->ilu && A->ilu->n == A->n && A->ilu->version == A->pattern_version) return GB300_OK;
   if(A->ilu) ilu_free(A->ilu);
   A->ilu = new ilu_data();
   ilu_data *L = A->ilu;
   L->n = A->n;
+  L->version = A->pattern_version;
   cudaStream_t st = A->ctx->stream;
   int n = A->n;
   DevBuf<int> indl, indu, err;
@@ -503,11 +506,21 @@ __global__ void k_cvt(long long n, const TI *__restrict__ in, TO *__restrict__ o
   if(i < n) out[i] = (TO)in[i];
 }
 
-// factor A's values (val) into the ILU(0) of the requested precision
-int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out)
+// factor A's values (val) into the ILU(0) of the requested precision; with
+// reuse, a factor of that precision already held for A's pattern is kept
+// (Re_Use_LU, as LinAlg_SolveAgain sets it: LinAlg_SPARSKIT.cpp:578-585)
+int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out,
+               bool reuse, int *factorized)
 {
   GB_TRY(ilu_setup(A));
   ilu_data *L = A->ilu;
+  if(factorized) *factorized = 0;
+  if(reuse && (fp32 ? L->fact32 : L->fact64)) {
+    *zero_row_out = 0;
+    return GB300_OK;
+  }
+  if(factorized) *factorized = 1;
+  L->fact32 = L->fact64 = false;
   cudaStream_t st = A->ctx->stream;
   int n = A->n;
   DevBuf<int> zr;
@@ -539,6 +552,7 @@ int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out)
   GB_CUDA(cudaStreamSynchronize(st));
   GB_CUDA(cudaGetLastError());
   *zero_row_out = (hz == big) ? 0 : hz;
+  if(!*zero_row_out) (fp32 ? L->fact32 : L->fact64) = true;
   return GB300_OK;
 }
 
@@ -985,7 +999,7 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   if(precond) {
     int zr = 0;
     // the factor is on A's values as given to the solver (scaled if needed)
-    GB_TRY(ilu_factor(A, val, fp32, &zr));
+    GB_TRY(ilu_factor(A, val, fp32, &zr, p->re_use_lu != 0, &info->ilu_factorized));
     if(zr) {
       info->status = zr;
       set_error("Zero pivot on line %d in ILU", zr);

@@ -68,7 +68,10 @@ void correction_apply(const gb300_matrix *A, const double *val, const double *v,
 
 // ILU(0) of A's pattern on the values val (FP64, or FP32 storage), and its
 // application z = M^-1 v guarded by *flag (gmres.cu)
-int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out);
+int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out,
+               bool reuse = false, int *factorized = nullptr);
+// drop the factor held by the multicolour copy of A (a new Generate)
+void colour_drop_factor(gb300_matrix *A);
 // rmask (optional): rows with rmask[i] == 0 are left out of the sweeps
 void ilu_apply(const gb300_matrix *A, bool fp32, const double *v, double *z,
                float *t32, const int *flag, cudaStream_t st,

@@ -59,20 +59,25 @@ __device__ __forceinline__ void tri3_curls(const Tri3Geo &g, double cx[3], doubl
   }
 }
 
-// unknown value of local DOF k (harmonic h): 0 for a fixed DOF
+// value of local DOF k (harmonic h of NH): the unknown's, or for a fixed
+// DOF its value (gfix, NH values per fixed DOF; 0 without a table)
 __device__ __forceinline__ double dof_value(const int *__restrict__ edofs, int nloc,
                                             int e, int k, int h,
-                                            const double *__restrict__ x)
+                                            const double *__restrict__ x,
+                                            const double *__restrict__ gfix = nullptr,
+                                            int nh = 1)
 {
   int d = edofs[(size_t)e * nloc + k];
-  return d >= 0 ? x[d + h] : 0.;
+  if(d >= 0) return x[d + h];
+  return gfix ? gfix[(size_t)(-d - 1) * nh + h] : 0.;
 }
 
 // b = {d a} per element: out[(e * NH + h) * 2 + c]
 template <int NH>
 __global__ void k_post_tri3(int ne, const double *__restrict__ nodes,
                             const int *__restrict__ elems, const int *__restrict__ edofs,
-                            const double *__restrict__ x, double *__restrict__ out)
+                            const double *__restrict__ x, double *__restrict__ out,
+                            const double *__restrict__ gfix)
 {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if(e >= ne) return;
@@ -84,7 +89,7 @@ __global__ void k_post_tri3(int ne, const double *__restrict__ nodes,
     double bx = 0., by = 0.;
 #pragma unroll
     for(int i = 0; i < 3; i++) {
-      double a = dof_value(edofs, 3, e, i, h, x);
+      double a = dof_value(edofs, 3, e, i, h, x, gfix, NH);
       bx += a * cx[i];
       by += a * cy[i];
     }
@@ -279,7 +284,8 @@ __global__ void k_post_points_tri3(int np, const double *__restrict__ xyz, Grid 
                                    const int *__restrict__ elems,
                                    const int *__restrict__ edofs,
                                    const double *__restrict__ x, double *__restrict__ fa,
-                                   double *__restrict__ fb, int *__restrict__ fe)
+                                   double *__restrict__ fb, int *__restrict__ fe,
+                                   const double *__restrict__ gfix)
 {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if(q >= np) return;
@@ -308,7 +314,7 @@ __global__ void k_post_points_tri3(int np, const double *__restrict__ xyz, Grid 
       tri3_curls(g, cx, cy);
       const double N[3] = {1. - bu - bv, bu, bv};
       for(int i = 0; i < 3; i++) {
-        double ai = dof_value(edofs, 3, best, i, h, x);
+        double ai = dof_value(edofs, 3, best, i, h, x, gfix, NH);
         a += N[i] * ai;
         bx += ai * cx[i];
         by += ai * cy[i];
@@ -381,7 +387,8 @@ __global__ void k_post_points_tet4_edge(int np, const double *__restrict__ xyz, 
 
 // ------------------------------------------------------------------- host
 struct PostIn {
-  DevBuf<double> nodes;
+  DevBuf<double> nodes, fixed;
+  const double *p_fixed = nullptr;
   DevBuf<int> elems, edofs;
   DevBuf<signed char> esign;
   const double *p_nodes = nullptr;
@@ -433,6 +440,15 @@ static int post_stage(cudaStream_t st, const gb300_term_batch *t, PostIn &I)
     set_error("edge elements need elem_sign");
     return GB300_ERR_ARG;
   }
+  if(t->fixed_values && t->n_fixed > 0) {
+    if(dim != 2) {
+      set_error("fixed DOF values are not supported for edge elements");
+      return GB300_ERR_UNSUPPORTED;
+    }
+    GB_TRY(check_fixed_table(st, I.p_edofs, (long long)ne * nloc, t->n_fixed));
+    GB_TRY(stage_in(st, t->fixed_values, (size_t)t->n_fixed * nh, t->on_device, I.fixed,
+                    &I.p_fixed));
+  }
   return GB300_OK;
 }
 
@@ -450,10 +466,10 @@ int post_elements(const gb300_term_batch *t, const gb300_vector *x, double *out)
   if(ne > 0) {
     if(t->kind == GB300_TERM_TRI3_MAGNETOSTATIC)
       k_post_tri3<1><<<grid_for(ne, 256), 256, 0, st>>>(ne, I.p_nodes, I.p_elems,
-                                                        I.p_edofs, x->d.p, d.p);
+                                                        I.p_edofs, x->d.p, d.p, I.p_fixed);
     else if(t->kind == GB300_TERM_TRI3_EDDY_COMPLEX)
       k_post_tri3<2><<<grid_for(ne, 256), 256, 0, st>>>(ne, I.p_nodes, I.p_elems,
-                                                        I.p_edofs, x->d.p, d.p);
+                                                        I.p_edofs, x->d.p, d.p, I.p_fixed);
     else
       k_post_tet4_edge<<<grid_for(ne, 256), 256, 0, st>>>(ne, I.p_nodes, I.p_elems,
                                                           I.p_edofs, I.p_esign, x->d.p,
@@ -537,11 +553,11 @@ int post_points(const gb300_term_batch *t, const gb300_vector *x, int np,
   if(t->kind == GB300_TERM_TRI3_MAGNETOSTATIC)
     k_post_points_tri3<1><<<grid_for(np, 128), 128, 0, st>>>(
       np, dxyz.p, G, ptr.p, list.p, I.p_nodes, I.p_elems, I.p_edofs, x->d.p, dfa.p, dfb.p,
-      dfe.p);
+      dfe.p, I.p_fixed);
   else if(t->kind == GB300_TERM_TRI3_EDDY_COMPLEX)
     k_post_points_tri3<2><<<grid_for(np, 128), 128, 0, st>>>(
       np, dxyz.p, G, ptr.p, list.p, I.p_nodes, I.p_elems, I.p_edofs, x->d.p, dfa.p, dfb.p,
-      dfe.p);
+      dfe.p, I.p_fixed);
   else
     k_post_points_tet4_edge<<<grid_for(np, 128), 128, 0, st>>>(
       np, dxyz.p, G, ptr.p, list.p, I.p_nodes, I.p_elems, I.p_edofs, I.p_esign, x->d.p,

@@ -52,5 +52,8 @@ int post_points(const gb300_term_batch *t, const gb300_vector *x, int np,
                 const double *xyz, double *field, double *curl, int *elem);
 int solve_batch(gb300_matrix *A, const gb300_vector *b, const gb300_solver_params *p,
                 gb300_vector *x, int nsys, const int *off, gb300_solve_info *infos);
+// GB300_ERR_ARG unless every negative entry e of the device table edofs (n
+// entries) names a fixed DOF of the table: -n_fixed <= e
+int check_fixed_table(cudaStream_t st, const int *edofs, long long n, int n_fixed);
 
 }  // namespace gb

@@ -203,3 +203,108 @@ def read_res(path: str, n: int) -> list:
         out.append((int(h[0]), float(h[1]), float(h[2]), int(h[3]), vals))
         pos = data.index(b"$EndSolution", k) + 12
     return out
+
+
+# --------------------------------------------------------------------------
+# .pre (DOF numbering) writer
+# --------------------------------------------------------------------------
+def dof_records(mesh, dm):
+    """Every DOF the element tables touch, as (NumType, Entity, Harmonic,
+    Type, NumDof, value) sorted by (NumType, Entity, Harmonic): GetDP's DOF
+    tree order (DofData.cpp:36-45).  Nodal spaces: NumType = component + 1,
+    Entity = node number; edge spaces: Entity = edge number (first-touch
+    order, dm.edges).  Type 1 unknown (NumDof 1-based), 2 fixed (with its
+    value: dm.fixed_values, or 0)."""
+    ed = np.asarray(dm.elem_dofs, np.int64)
+    ne, nloc = ed.shape
+    fv = None if dm.fixed_values is None else np.asarray(dm.fixed_values, np.float64)
+    if dm.edges is not None:  # Whitney edges: local edge k of the element
+        from .workloads import TET4_EDGES
+        nn = mesh.n_nodes
+        ve = mesh.elems[:, TET4_EDGES].reshape(-1, 2).astype(np.int64)
+        key = np.minimum(ve[:, 0], ve[:, 1]) * nn + np.maximum(ve[:, 0], ve[:, 1])
+        ekey = dm.edges[:, 0].astype(np.int64) * nn + dm.edges[:, 1]
+        order = np.argsort(ekey)
+        ent = order[np.searchsorted(ekey[order], key)] + 1
+        numtype = np.ones_like(ent)
+        flat = ed.ravel()
+        harm = [(0, flat)]
+    else:
+        nv = mesh.elems.shape[1]
+        comp = np.arange(nloc) // nv
+        ent = (mesh.elems[:, np.arange(nloc) % nv].astype(np.int64) + 1).ravel()
+        numtype = np.broadcast_to(comp + 1, (ne, nloc)).ravel()
+        flat = ed.ravel()
+        harm = [(h, flat) for h in range(dm.nharm)]
+    recs = []
+    for h, d in harm:
+        unk = d >= 0
+        num = np.where(unk, d + h + 1, 0)  # 1-based; harmonic 1 is the next number
+        if fv is None:
+            val = np.zeros(len(d))
+        else:
+            k = np.maximum(-d - 1, 0)
+            val = fv[k, h] if fv.ndim == 2 else (fv[k] if h == 0 else np.zeros(len(d)))
+            val = np.where(unk, 0.0, val)
+        recs.append(np.stack([numtype, ent, np.full(len(d), h), np.where(unk, 1, 2),
+                              num, val], 1))
+    r = np.concatenate(recs)
+    key = r[:, :3].astype(np.int64)
+    _, first = np.unique(key, axis=0, return_index=True)
+    return r[first]
+
+
+def write_pre(path: str, mesh, dm, resolution: str = "R", n_spaces: int = None) -> None:
+    """The .pre file GetDP writes for a one-system resolution
+    (Dof_WriteFilePRE, DofData.cpp:363-462): the $Resolution header, one
+    $DofData block (resolution and system index 0, the function spaces
+    0..n-1, time function 0), every DOF of the tree with its number (unknown)
+    or value (fixed, "%.16g" as LinAlg_PrintScalar prints it)."""
+    r = dof_records(mesh, dm)
+    if n_spaces is None:
+        n_spaces = int(r[:, 0].max()) if len(r) else 1
+    n_unknown = int(np.sum(r[:, 3] == 1))
+    out = [f"$Resolution /* '{resolution}' */", "0 1", "$EndResolution",
+           "$DofData /* #0 */", "0 0",
+           " ".join([str(n_spaces)] + [str(i) for i in range(n_spaces)]),
+           "1 0", "1 0", f"{len(r)} {n_unknown}"]
+    for nt, ent, h, typ, num, val in r:
+        if int(typ) == 1:
+            out.append(f"{int(nt)} {int(ent)} {int(h)} 1 {int(num)} 1")
+        else:
+            out.append(f"{int(nt)} {int(ent)} {int(h)} 2 {'%.16g' % val} 0")
+    out.append("$EndDofData")
+    if dm.edges is not None:
+        out.extend(_elements_x_edges(mesh, dm))
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")
+
+
+def _elements_x_edges(mesh, dm):
+    """$ElementsXEdges (Geo_WriteFilePRE, GeoEntity.cpp:526-552): every
+    element with edges, in mesh order (volume elements, then the boundary
+    elements whose edges the constraint created), with its edges' numbers,
+    negative where the element runs the edge from the higher to the lower
+    node number (GeoEntity.h:214-215 local edges)."""
+    from .workloads import TET4_EDGES, TRI3_EDGES_GETDP
+    nn = mesh.n_nodes
+    ekey = dm.edges[:, 0].astype(np.int64) * nn + dm.edges[:, 1]
+    order = np.argsort(ekey)
+
+    def signed(conn, loc):
+        ve = conn[:, loc].reshape(-1, 2).astype(np.int64)
+        key = np.minimum(ve[:, 0], ve[:, 1]) * nn + np.maximum(ve[:, 0], ve[:, 1])
+        num = order[np.searchsorted(ekey[order], key)] + 1
+        return np.where(ve[:, 0] < ve[:, 1], num, -num).reshape(len(conn), -1)
+
+    blocks = [signed(mesh.elems, TET4_EDGES)]
+    if len(mesh.bnd):
+        blocks.append(signed(mesh.bnd, TRI3_EDGES_GETDP))
+    lines = ["$ElementsXEdges", f"0 {sum(len(b) for b in blocks)}"]
+    i = 0
+    for blk in blocks:
+        for row in blk:
+            lines.append(f"{i} {len(row)} " + " ".join(str(int(v)) for v in row))
+            i += 1
+    lines.append("$EndElementsXEdges")
+    return lines

@@ -57,6 +57,8 @@ def term_arrays(p: Problem, dm: DofMap) -> dict:
         p0 = p.params["reg"]
     else:
         raise ValueError(f)
+    if dm.fixed_values is not None:
+        a["fixed_values"] = np.ascontiguousarray(dm.fixed_values, np.float64)
     a["_kind"] = kind
     a["_p"] = (p0, p1, p2)
     return a
@@ -68,8 +70,10 @@ def _batch(arrays: dict, ptrs: dict, on_device: int) -> TermBatch:
     t.n_nodes = arrays["nodes"].shape[0]
     t.n_elems = arrays["elems"].shape[0]
     for k in ("nodes", "elems", "elem_dofs", "elem_sign", "coef", "source", "coef2",
-              "coef3"):
+              "coef3", "fixed_values"):
         setattr(t, k, ptrs.get(k))
+    fv = arrays.get("fixed_values")
+    t.n_fixed = 0 if fv is None else fv.shape[0]
     t.p0, t.p1, t.p2 = arrays["_p"]
     t.on_device = on_device
     return t
@@ -114,10 +118,14 @@ def host_batch(arrays: dict) -> TermBatch:
 
 
 def generate(A: gMatrix, b: gVector, batch: TermBatch, pattern: bool = True,
-             solution: gVector = None) -> None:
-    """Generate[A]: (re)build A's pattern if asked, zero A and b, assemble
-    (at the current solution, for a formulation that depends on it)."""
+             solution: gVector = None, scatter: int = None) -> None:
+    """Generate[A]: (re)build A's pattern if asked (a pattern this context
+    built from the same element table is reused), zero A and b, assemble (at
+    the current solution, for a formulation that depends on it).  scatter:
+    one of _lib.SCATTER_* (default: the batch's own setting)."""
     L = _lib.load()
+    if scatter is not None:
+        batch.scatter = int(scatter)
     if pattern:
         check(L.gb300_generate_pattern(A.h, ctypes.byref(batch)))
     else:

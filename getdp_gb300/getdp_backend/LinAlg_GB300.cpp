@@ -724,12 +724,32 @@ void LinAlg_AssembleMatrix(gMatrix *M) { ok(gb300_matrix_assemble(M->M)); }
 
 void LinAlg_AssembleVector(gVector *V) {}
 
+// Sparskit's threshold and level-of-fill ILUs (Preconditioner 1 ILUT,
+// 2 ILUTP -- the default of Sparskit.cpp:1854 --, 3 ILUD, 4 ILUDP, 5 ILUK,
+// 7 MILU0) have no GPU counterpart here: the solve runs with ILU(0)
+// (Preconditioner 6) and says so once per run.
+static gb300_solver_params gpu_params(const gb300_solver_params &p)
+{
+  gb300_solver_params q = p;
+  if((p.preconditioner >= 1 && p.preconditioner <= 5) || p.preconditioner == 7) {
+    static int warned = 0;
+    if(!warned) {
+      Message::Warning("GB300 backend: Preconditioner %d is not available on the GPU; "
+                       "ILU(0) (Preconditioner 6) is used instead", p.preconditioner);
+      warned = 1;
+    }
+    q.preconditioner = 6;
+  }
+  return q;
+}
+
 void LinAlg_Solve(gMatrix *A, gVector *B, gSolver *Solver, gVector *X,
                   int solverIndex)
 {
   gb300_solve_info info;
   dev(B);
-  int rc = gb300_solve(A->M, B->D, &Solver->Params, X->D, &info);
+  gb300_solver_params params = gpu_params(Solver->Params);
+  int rc = gb300_solve(A->M, B->D, &params, X->D, &info);
   X->state = DEV;
   if(rc == GB300_ERR_SOLVER)  // Sparskit only warns when iterations fail
     Message::Warning("Iterative solver terminated (code = %d)", info.status);
@@ -739,10 +759,15 @@ void LinAlg_Solve(gMatrix *A, gVector *B, gSolver *Solver, gVector *X,
                 info.true_residual);
 }
 
+// the factorisation of the previous solve of A is reused, as the reference
+// sets Re_Use_LU for this call (LinAlg_SPARSKIT.cpp:578-585)
 void LinAlg_SolveAgain(gMatrix *A, gVector *B, gSolver *Solver, gVector *X,
                        int solverIndex)
 {
+  int tmp = Solver->Params.re_use_lu;
+  Solver->Params.re_use_lu = 1;
   LinAlg_Solve(A, B, Solver, X, solverIndex);
+  Solver->Params.re_use_lu = tmp;
 }
 
 void LinAlg_SolveNL(gMatrix *A, gVector *B, gMatrix *J, gVector *R,

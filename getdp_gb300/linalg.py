@@ -336,4 +336,11 @@ def LinAlg_SolveBatch(A: gMatrix, B: gVector, Solver: gSolver, X: gVector,
 
 def LinAlg_SolveAgain(A: gMatrix, B: gVector, Solver: gSolver, X: gVector,
                       solverIndex: int = 0) -> dict:
-    return LinAlg_Solve(A, B, Solver, X, solverIndex)
+    """LinAlg_Solve reusing the previous solve's ILU(0) factorisation of A
+    (Re_Use_LU set for this call, LinAlg_SPARSKIT.cpp:578-585)."""
+    keep = Solver["re_use_lu"]
+    Solver["re_use_lu"] = 1
+    try:
+        return LinAlg_Solve(A, B, Solver, X, solverIndex)
+    finally:
+        Solver["re_use_lu"] = keep

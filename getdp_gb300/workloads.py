@@ -183,7 +183,8 @@ class Problem:
     params: dict
 
 
-def magnetostatics_2d(n: int, seed: int = 1, jitter: float = 0.2) -> Problem:
+def magnetostatics_2d(n: int, seed: int = 1, jitter: float = 0.2,
+                      dirichlet=None) -> Problem:
     """a_z nodal P1 magnetostatics on the unit square (BF_PerpendicularEdge).
 
     nu = 1/(mu0*mu_r), mu_r = 1000 inside the disk r < 0.25 about (0.5, 0.5);
@@ -204,7 +205,7 @@ def magnetostatics_2d(n: int, seed: int = 1, jitter: float = 0.2) -> Problem:
     js[reg == 3] = 1.0e6
     js[reg == 4] = -1.0e6
     return Problem(f"magnetostatics2d_n{n}", m, "magnetostatics2d", nu, js,
-                   {"n": n, "seed": seed, "jitter": jitter})
+                   {"n": n, "seed": seed, "jitter": jitter, "dirichlet": dirichlet})
 
 
 def gaussian_field(points: np.ndarray, seed: int, corr: float,
@@ -226,7 +227,7 @@ def gaussian_field(points: np.ndarray, seed: int, corr: float,
 
 def nonlinear_2d(n: int, seed: int = 5, jitter: float = 0.2, corr: float = 0.05,
                  sigma_log: float = 1.0, n_blobs: int = 8,
-                 blob_radius: float = 0.02) -> Problem:
+                 blob_radius: float = 0.02, dirichlet=None) -> Problem:
     """Nonlinear a_z P1 magnetostatics on the unit square.
 
     nu(x, |B|) = nu0(x) (1 + 999 exp(-|B|^2 / 1.5^2))^-1 with nu0 =
@@ -251,10 +252,11 @@ def nonlinear_2d(n: int, seed: int = 5, jitter: float = 0.2, corr: float = 0.05,
     m.region = np.full(m.n_elems, 1, np.int32)
     return Problem(f"nonlinear2d_n{n}", m, "nonlinear2d", nu0, js,
                    {"n": n, "seed": seed, "jitter": jitter, "b_sat2": 1.5 ** 2,
-                    "k_sat": 999.0})
+                    "k_sat": 999.0, "dirichlet": dirichlet})
 
 
-def elasticity_p2(n: int, seed: int = 2, sigma_log: float = 0.5) -> Problem:
+def elasticity_p2(n: int, seed: int = 2, sigma_log: float = 0.5,
+                  dirichlet=None) -> Problem:
     """3D linear elasticity, 10-node tetrahedra, per-element lognormal E.
 
     Unit cube of n^3 hexes x 6 Kuhn tets; E median 200 GPa, sigma_log 0.5;
@@ -270,7 +272,7 @@ def elasticity_p2(n: int, seed: int = 2, sigma_log: float = 0.5) -> Problem:
     return Problem(f"elasticity_p2_n{n}", m, "elasticity", E,
                    np.zeros(len(tet10)),
                    {"n": n, "seed": seed, "poisson": 0.3, "rho": 7800.0,
-                    "g": 9.81})
+                    "g": 9.81, "dirichlet": dirichlet})
 
 
 # Analytic potential of the toroidal source current: T = h(z) Psi(r) e_z about
@@ -363,7 +365,7 @@ def curlcurl_edge(n: int, seed: int = 3) -> Problem:
 
 
 def eddy_2d(n: int, seed: int = 4, freq: Optional[float] = None,
-            jitter: float = 0.2) -> Problem:
+            jitter: float = 0.2, dirichlet=None) -> Problem:
     """Complex (time-harmonic) a_z P1 eddy-current problem on the unit square.
 
     sigma = 5.8e7 S/m in 1-4 seeded disks (radius 0.05-0.15), frequency
@@ -393,7 +395,7 @@ def eddy_2d(n: int, seed: int = 4, freq: Optional[float] = None,
     js[reg == 4] = -1.0e6
     return Problem(f"eddy2d_n{n}", m, "eddy2d", nu, js,
                    {"n": n, "seed": seed, "freq": freq, "sigma": sigma,
-                    "disks": disks})
+                    "disks": disks, "dirichlet": dirichlet})
 
 
 # --------------------------------------------------------------------------
@@ -415,13 +417,48 @@ class DofMap:
     ncomp: int = 1
     nharm: int = 1
     edges: Optional[np.ndarray] = None  # (n_edges, 2) global edge nodes
+    # non-homogeneous Dirichlet: fixed DOF k has value fixed_values[k]
+    # ((n_fixed, 2) re/im for two harmonics) and elem_dofs holds -1-k for it;
+    # None when every fixed DOF is 0 (elem_dofs then holds -1)
+    fixed_values: Optional[np.ndarray] = None
 
 
-def nodal_dofmap(m: Mesh, ncomp: int = 1, nharm: int = 1) -> DofMap:
-    """BF_Node / BF_PerpendicularEdge on NodesOf[All] with a = 0 on the
-    boundary group.  Unknowns: (component, node, harmonic) sorted, i.e.
-    component-major across function spaces (their basis functions carry
-    increasing NumType) and harmonic-minor (DofData.cpp:1287-1295)."""
+# Named sets of non-homogeneous Dirichlet data, one (c0, cx, cy, cz) per
+# field component: a generator's ``dirichlet`` may be a set number.
+DIRICHLET_SETS = {
+    1: [(1.0e-3, 2.0e-3, -1.5e-3, 0.0)],                    # a_z (2D)
+    2: [(0.0, 0.0, 0.0, 0.0), (0.0, 0.0, 0.0, 0.0),
+        (0.0, 0.0, -2.0e-5, 1.0e-5)],                        # (ux, uy, uz)
+}
+
+
+def dirichlet_coefs(g):
+    """None, a DIRICHLET_SETS number, or per-component coefficient tuples."""
+    if g is None:
+        return None
+    return DIRICHLET_SETS[int(g)] if isinstance(g, (int, np.integer)) else g
+
+
+def dirichlet_values(nodes: np.ndarray, coefs) -> np.ndarray:
+    """g = c0 + cx X + cy Y + cz Z at the nodes, evaluated left to right as
+    GetDP evaluates the constraint expression written by constraint_expr."""
+    c0, cx, cy, cz = coefs
+    return c0 + cx * nodes[:, 0] + cy * nodes[:, 1] + cz * nodes[:, 2]
+
+
+def constraint_expr(coefs) -> str:
+    c0, cx, cy, cz = coefs
+    return f"{c0!r} + {cx!r}*X[] + {cy!r}*Y[] + {cz!r}*Z[]"
+
+
+def nodal_dofmap(m: Mesh, ncomp: int = 1, nharm: int = 1, dirichlet=None) -> DofMap:
+    """BF_Node / BF_PerpendicularEdge on NodesOf[All] with the boundary group
+    fixed: a = 0, or with ``dirichlet`` (one (c0, cx, cy, cz) per component)
+    a = c0 + cx X + cy Y + cz Z at each fixed node (real for two harmonics).
+    Unknowns: (component, node, harmonic) sorted, i.e. component-major across
+    function spaces (their basis functions carry increasing NumType) and
+    harmonic-minor (DofData.cpp:1287-1295).  Fixed DOFs with values are
+    numbered component by component in node order."""
     used = np.zeros(m.n_nodes, bool)
     used[m.elems.ravel()] = True
     fixed = np.zeros(m.n_nodes, bool)
@@ -433,19 +470,30 @@ def nodal_dofmap(m: Mesh, ncomp: int = 1, nharm: int = 1) -> DofMap:
     nloc = m.elems.shape[1]
     # local DOF order: component-major over the element's nodes (GetDP keeps
     # one QuantityStorage per quantity; each Galerkin term uses one of them)
+    fnum = np.full(m.n_nodes, -1, np.int64)
+    fixed_nodes = np.flatnonzero(used & fixed)
+    fnum[fixed_nodes] = np.arange(len(fixed_nodes))
+    nf = len(fixed_nodes)
     blocks = []
     for c in range(ncomp):
         for h in range(nharm):
             base = num[m.elems]
-            blocks.append(np.where(base >= 0, (c * nu + base) * nharm + h, -1))
+            fx = -1 if dirichlet is None else -1 - (c * nf + fnum[m.elems])
+            blocks.append(np.where(base >= 0, (c * nu + base) * nharm + h, fx))
     if nharm == 1:
         dofs = np.concatenate(blocks, axis=1)
     else:
         # complex: harmonic pairs are consecutive numbers; keep harmonic 0 in
         # the table (the assembly adds harmonic 1 as +1)
         dofs = np.concatenate(blocks[0::nharm], axis=1)
+    fv = None
+    if dirichlet is not None:
+        fv = np.concatenate([dirichlet_values(m.nodes[fixed_nodes], dirichlet[c])
+                             for c in range(ncomp)])
+        if nharm == 2:
+            fv = np.stack([fv, np.zeros_like(fv)], 1)
     return DofMap(nu * ncomp * nharm, dofs.astype(np.int32),
-                  np.ones(dofs.shape, np.int8), ncomp, nharm)
+                  np.ones(dofs.shape, np.int8), ncomp, nharm, fixed_values=fv)
 
 
 TET4_EDGES = np.array([[0, 1], [0, 2], [0, 3], [1, 2], [1, 3], [2, 3]])
@@ -494,14 +542,15 @@ def edge_dofmap(m: Mesh) -> DofMap:
 
 
 def dofmap_for(p: Problem) -> DofMap:
+    g = dirichlet_coefs(p.params.get("dirichlet"))
     if p.formulation == "magnetostatics2d":
-        return nodal_dofmap(p.mesh)
+        return nodal_dofmap(p.mesh, dirichlet=g)
     if p.formulation == "eddy2d":
-        return nodal_dofmap(p.mesh, nharm=2)
+        return nodal_dofmap(p.mesh, nharm=2, dirichlet=g)
     if p.formulation == "nonlinear2d":
-        return nodal_dofmap(p.mesh)
+        return nodal_dofmap(p.mesh, dirichlet=g)
     if p.formulation == "elasticity":
-        return nodal_dofmap(p.mesh, ncomp=3)
+        return nodal_dofmap(p.mesh, ncomp=3, dirichlet=g)
     if p.formulation == "curlcurl":
         return edge_dofmap(p.mesh)
     raise ValueError(p.formulation)
@@ -602,6 +651,13 @@ def write_msh22(m: Mesh, path: str) -> None:
 _DUMP_OPS = ('Generate[A]; Write[A, File "b.bin"]; Solve[A]; SaveSolution[A];')
 
 
+def _cvalue(p: Problem, comp: int) -> str:
+    """The Value of a fixed-DOF constraint: 0., or the expression of the
+    problem's Dirichlet coefficients for that component."""
+    g = dirichlet_coefs(p.params.get("dirichlet"))
+    return "0." if g is None else constraint_expr(g[comp])
+
+
 def pro_text(p: Problem) -> str:
     """A GetDP problem file for p, using the canonical Galerkin terms the
     GPU kernels implement.  Per-element coefficients that vary element by
@@ -639,7 +695,7 @@ def pro_text(p: Problem) -> str:
 Function {{
   {chr(10).join('  ' + s for s in fun)}
 }}
-Constraint {{ {{ Name a; Case {{ {{ Region Bnd; Value 0.; }} }} }} }}
+Constraint {{ {{ Name a; Case {{ {{ Region Bnd; Value {_cvalue(p, 0)}; }} }} }} }}
 FunctionSpace {{
   {{ Name Hcurl_a; Type Form1P;
     BasisFunction {{ {{ Name se; NameOfCoef ae; Function BF_PerpendicularEdge;
@@ -677,7 +733,7 @@ Function {{
              (1. + {ks:.17g} * Exp[-SquNorm[$1] / {b2:.17g}])^2;
   dhdb[] = TensorDiag[1, 1, 1] * nu[$1] + 2. * dnudb2[$1] * SquDyadicProduct[$1];
 }}
-Constraint {{ {{ Name a; Case {{ {{ Region Bnd; Value 0.; }} }} }} }}
+Constraint {{ {{ Name a; Case {{ {{ Region Bnd; Value {_cvalue(p, 0)}; }} }} }} }}
 FunctionSpace {{
   {{ Name Hcurl_a; Type Form1P;
     BasisFunction {{ {{ Name se; NameOfCoef ae; Function BF_PerpendicularEdge;
@@ -728,7 +784,9 @@ Resolution {{ {{ Name R; System {{ {{ Name A; NameOfFormulation F; }} }}
             spaces.append(f"""  {{ Name H_u{c}; Type Form0;
     BasisFunction {{ {{ Name s{c}; NameOfCoef u{c}n; Function BF_Node;
       Support Vol; Entity NodesOf[All]; }} }}
-    Constraint {{ {{ NameOfCoef u{c}n; EntityType NodesOf; NameOfConstraint Clamp; }} }} }}""")
+    Constraint {{ {{ NameOfCoef u{c}n; EntityType NodesOf; NameOfConstraint Clamp{c}; }} }} }}""")
+        clamps = " ".join(f"{{ Name Clamp{c}; Case {{ {{ Region Fix; Value {_cvalue(p, k)}; }} }} }}"
+                          for k, c in enumerate(comps))
         return f"""Group {{
   Vol = Region[{{{1000}:{1000 + ne - 1}}}]; Fix = Region[20];
 }}
@@ -749,7 +807,7 @@ Function {{
   C_zz[] = Tensor[ b[],0  ,0  ,    0  ,b[],0  ,    0  ,0  ,a[] ];
   f[] = Vector[0, 0, {-rhog:.17g}];
 }}
-Constraint {{ {{ Name Clamp; Case {{ {{ Region Fix; Value 0.; }} }} }} }}
+Constraint {{ {clamps} }}
 FunctionSpace {{
 {chr(10).join(spaces)}
 }}

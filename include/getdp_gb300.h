@@ -113,6 +113,9 @@ typedef struct gb300_solve_info {
   double rhs_norm;       /* ||b||_2 of that system */
   int refinement_steps;  /* FP64 refinement steps (Precision 1) */
   int inner_iterations;  /* FP32 inner iterations (Precision 1) */
+  int ilu_factorized;    /* 1: this solve computed an ILU(0) factorisation;
+                            0: none, or the previous one was reused
+                            (Re_Use_LU, as LinAlg_SolveAgain sets it) */
 } gb300_solve_info;
 
 /* ---- vectors (device resident, FP64) -------------------------------- */
@@ -215,7 +218,33 @@ typedef struct gb300_term_batch {
                                     batch can carry a frequency sweep */
   double p0, p1, p2;
   int on_device;                 /* 1: the arrays above are device pointers */
+  /* Fixed DOFs with values (the Dirichlet elimination of Dof_AssembleInMat,
+     DofData.cpp:1489-1542): NULL when every fixed DOF is 0 (any negative
+     elem_dofs entry is then a fixed zero).  Otherwise a negative entry e
+     names fixed DOF -e-1 of value fixed_values[-e-1] (TRI3_EDDY_COMPLEX: two
+     values per fixed DOF, real and imaginary part), and every unknown row i
+     of the element gets b_i += (g_j * 1) * -Ek_ij.  Supported by the TRI3
+     kinds and TET10_ELASTICITY (the nonlinear kind also evaluates {d a}
+     with them). */
+  const double *fixed_values;
+  int n_fixed;
+  /* How element contributions are added into A and b (GB300_SCATTER_*):
+     DEFAULT is TABLE where one exists, else SEARCH.  SEARCH finds each
+     entry by a binary search in its sorted row and adds with FP64 atomics;
+     TABLE (node-blocked P2 elasticity on a pattern this context's
+     gb300_generate_pattern built) reads the offsets from a table made once
+     per pattern and adds with atomics; COLOURED launches the elements colour
+     by colour (no two elements of a colour share an unknown; the colouring
+     is made once per pattern) and adds without atomics, so that A and b are
+     the same to the last bit on every run.  Atomics make the order of the
+     additions into one entry vary between runs (rounding only). */
+  int scatter;
 } gb300_term_batch;
+
+#define GB300_SCATTER_DEFAULT 0
+#define GB300_SCATTER_SEARCH 1
+#define GB300_SCATTER_TABLE 2
+#define GB300_SCATTER_COLOURED 3
 
 /* Build the CSR pattern of A from the element tables (rows of unknowns
    touched by each element, sorted, no duplicates: the pattern the
@@ -279,6 +308,9 @@ int gb300_bench_spmv(gb300_matrix *A, int precision, int reps, double *ms);
    flops per FMA): the denominator of the FP64-bound element kernels'
    roofline. */
 int gb300_bench_fp64_peak(gb300_ctx *ctx, double *tflops);
+/* The same for FP64 tensor-core instructions (mma.sync m8n8k4 f64): whether
+   DMMA would raise the FP64-bound element kernels' ceiling. */
+int gb300_bench_dmma_peak(gb300_ctx *ctx, double *tflops);
 
 /* ---- residual without device allocation ------------------------------ */
 /* No counterpart in the reference: an entry point for callers that cannot

@@ -110,6 +110,18 @@ def assemble_coo(problem, dofmap, ilu: str = "64", solution=None):
     """The matrix contributions in the reference's call order (the
     LinAlg_AddDoubleInMatrix sequence) and the RHS: (rows, cols, vals, b)."""
     L = lib(ilu)
+    fixed = getattr(dofmap, "fixed_values", None)
+    if fixed is not None:
+        fixed = np.ascontiguousarray(fixed, np.float64)
+        L.oracle_set_fixed(_p(fixed, ctypes.c_double))
+    try:
+        return _assemble_coo(L, problem, dofmap, solution)
+    finally:
+        if fixed is not None:
+            L.oracle_set_fixed(None)
+
+
+def _assemble_coo(L, problem, dofmap, solution):
     m = problem.mesh
     n = dofmap.n_dof
     ne = m.n_elems

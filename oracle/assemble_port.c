@@ -60,6 +60,28 @@ static void badd(double *b, int row, double v)
   if(g_babs) g_babs[row] += fabs(v);
 }
 
+/* the same with the rounding scale of v given (a sum whose terms cancel) */
+static void badd_scaled(double *b, int row, double v, double scale)
+{
+  b[row] += v;
+  if(g_babs) g_babs[row] += scale;
+}
+
+/* the rounding scale of an addition the reference skips (an element matrix
+   entry that is exactly 0 here may be rounding residue in another
+   evaluation order) */
+static void bscale(int row, double scale)
+{
+  if(g_babs) g_babs[row] += scale;
+}
+
+/* Values of the fixed DOFs (NULL: every fixed DOF is 0).  With a table, a
+   negative DOF entry d names fixed DOF -d-1 (2 values, re and im, in the
+   complex formulation), and Dof_AssembleInMat's elimination
+   (DofData.cpp:1489-1542) adds b_i += (g_j * TF) * -Ek_ij, TF = 1. */
+static const double *g_fix = NULL;
+void oracle_set_fixed(const double *gfix) { g_fix = gfix; }
+
 /* COO sink in call order */
 typedef struct {
   int64_t n, cap;
@@ -265,6 +287,7 @@ int64_t oracle_assemble_tri3_nl(int ne, const double *nodes, const int *elems,
     const int *el = elems + 3 * e;
     const int *dof = edofs + 3 * e;
     double Ek[3][3], Eb1[3] = {0., 0., 0.}, Eb3[3] = {0., 0., 0.};
+    double Sb1[3] = {0., 0., 0.}, Sb3[3] = {0., 0., 0.};  /* sums of |terms| */
     double x[3], y[3], n[3], D, F;
     M3 J;
     for(i = 0; i < 3; i++)
@@ -273,9 +296,13 @@ int64_t oracle_assemble_tri3_nl(int ne, const double *nodes, const int *elems,
       double cE[3][3], bv[3] = {0., 0., 0.}, T[3][3], nu, hb[3], tb[3];
       tri_geom(nodes, el, q, x, y, &J, &D, n);
       for(i = 0; i < 3; i++) tri_curl(&J, D, i, cE[i]);
+      double bs[3] = {0., 0., 0.};  /* rounding scale of the field */
       for(i = 0; i < 3; i++) {
-        double a = dof[i] >= 0 ? sol[dof[i]] : 0.;
-        for(c = 0; c < 3; c++) bv[c] += a * cE[i][c];
+        double a = dof[i] >= 0 ? sol[dof[i]] : (g_fix ? g_fix[-dof[i] - 1] : 0.);
+        for(c = 0; c < 3; c++) {
+          bv[c] += a * cE[i][c];
+          bs[c] += fabs(a * cE[i][c]);
+        }
       }
       nl_law(nu0[e], k, b2, bv, &nu, T);
       F = 1. * (PT3[q] * fabs(D));
@@ -286,6 +313,16 @@ int64_t oracle_assemble_tri3_nl(int ne, const double *nodes, const int *elems,
       for(i = 0; i < 3; i++) {
         Eb1[i] += F * dot3(cE[i], hb);
         Eb3[i] += F * dot3(cE[i], tb);
+        /* the field's own rounding (nodal values cancel in the curl) enters
+           nu and dhdb with the law's sensitivity 1 + 2 |b|^2 / b2 */
+        {
+          double sens = 1. + 2. * (bv[0] * bv[0] + bv[1] * bv[1]) / b2;
+          for(c = 0; c < 3; c++) {
+            double tsc = fabs(T[c][0]) * bs[0] + fabs(T[c][1]) * bs[1] + fabs(T[c][2]) * bs[2];
+            Sb1[i] += F * fabs(cE[i][c]) * (fabs(nu) * bs[c]) * sens;
+            Sb3[i] += F * fabs(cE[i][c]) * tsc * sens;
+          }
+        }
         for(j = 0; j < 3; j++) {
           double tc[3];
           for(c = 0; c < 3; c++)
@@ -295,12 +332,20 @@ int64_t oracle_assemble_tri3_nl(int ne, const double *nodes, const int *elems,
       }
     }
     for(i = 0; i < 3; i++)
-      if(dof[i] >= 0 && Eb1[i]) badd(b, dof[i], (1. * 1.) * -Eb1[i]);
+      if(dof[i] >= 0 && Eb1[i]) badd_scaled(b, dof[i], (1. * 1.) * -Eb1[i], Sb1[i]);
     for(i = 0; i < 3; i++)
-      for(j = 0; j < 3; j++)
+      for(j = 0; j < 3; j++) {
         if(dof[i] >= 0 && dof[j] >= 0) coo_add(&m, dof[i], dof[j], Ek[i][j]);
+        else if(dof[i] >= 0 && g_fix) {
+          double sc = fabs(g_fix[-dof[j] - 1]) * sqrt(fabs(Ek[i][i] * Ek[j][j]));
+          if(Ek[i][j])
+            badd_scaled(b, dof[i], (g_fix[-dof[j] - 1] * 1.) * -Ek[i][j], sc);
+          else
+            bscale(dof[i], sc);
+        }
+      }
     for(i = 0; i < 3; i++)
-      if(dof[i] >= 0 && Eb3[i]) badd(b, dof[i], (1. * 1.) * -Eb3[i]);
+      if(dof[i] >= 0 && Eb3[i]) badd_scaled(b, dof[i], (1. * 1.) * -Eb3[i], Sb3[i]);
     if(js[e] != 0.) {
       double Es[3] = {0., 0., 0.};
       for(q = 0; q < 3; q++) {
@@ -347,7 +392,23 @@ int64_t oracle_assemble_tri_p1(int ne, const double *nodes, const int *elems,
       for(j = 0; j < i; j++) Ek[j][i] = Ek[i][j];
     for(i = 0; i < 3; i++)
       for(j = 0; j < 3; j++) {
-        if(dof[i] < 0 || dof[j] < 0) continue; /* fixed: b += 0 */
+        if(dof[i] >= 0 && dof[j] < 0 && g_fix) { /* fixed: elimination */
+          int f = -dof[j] - 1;
+          double sc = sqrt(fabs(Ek[i][i] * Ek[j][j]));  /* rounding scale of Ek_ij */
+          if(!complex_mode) {
+            if(Ek[i][j])
+              badd_scaled(b, dof[i], (g_fix[f] * 1.) * -Ek[i][j], fabs(g_fix[f]) * sc);
+            else
+              bscale(dof[i], fabs(g_fix[f]) * sc);
+          }
+          else { /* Val = (Ek, 0): valtmp = (-d1 Val0 + d2 Val1, -d1 Val1 - d2 Val0) */
+            double d1 = g_fix[2 * f] * 1., d2 = g_fix[2 * f + 1] * 1.;
+            double gs = (fabs(d1) + fabs(d2)) * sc;
+            badd_scaled(b, dof[i], -d1 * Ek[i][j] + d2 * 0., gs);
+            badd_scaled(b, dof[i] + 1, -d1 * 0. - d2 * Ek[i][j], gs);
+          }
+        }
+        if(dof[i] < 0 || dof[j] < 0) continue;
         if(!complex_mode)
           coo_add(&m, dof[i], dof[j], Ek[i][j]);
         else if(Ek[i][j]) { /* AddComplexInMatrix, imaginary part 0 */
@@ -373,6 +434,13 @@ int64_t oracle_assemble_tri_p1(int ne, const double *nodes, const int *elems,
       for(i = 0; i < 3; i++)
         for(j = 0; j < 3; j++) {
           double d1 = -0. * omega, d2 = Ek[i][j] * omega;
+          if(dof[i] >= 0 && dof[j] < 0 && g_fix) { /* Val = (d1, d2) */
+            int f = -dof[j] - 1;
+            double g1 = g_fix[2 * f] * 1., g2 = g_fix[2 * f + 1] * 1.;
+            double gs = (fabs(g1) + fabs(g2)) * omega * sqrt(fabs(Ek[i][i] * Ek[j][j]));
+            badd_scaled(b, dof[i], -g1 * d1 + g2 * d2, gs);
+            badd_scaled(b, dof[i] + 1, -g1 * d2 - g2 * d1, gs);
+          }
           if(dof[i] < 0 || dof[j] < 0) continue;
           if(d1) { /* never: the mass term is real */
             coo_add(&m, dof[i], dof[j], d1);
@@ -462,6 +530,22 @@ int64_t oracle_assemble_tet10_elasticity(int ne, const double *nodes,
       for(i = 0; i < 10; i++) form1(&I, dndu[i], gx[q][i]);
       Fq[q] = 1. * (PTET4[q] * fabs(D));
     }
+    /* with the RHS scale accumulator and fixed values: the diagonal of each
+       component's (c, c) term, the rounding scale of the eliminations */
+    double Dg[3][10];
+    if(g_babs && g_fix)
+      for(ci = 0; ci < 3; ci++) {
+        double T[9];
+        lame_tensor(E[e], poisson, ci, ci, T);
+        for(i = 0; i < 10; i++) {
+          Dg[ci][i] = 0.;
+          for(q = 0; q < 4; q++) {
+            double cD[3];
+            tensor_vec(T, gx[q][i], cD);
+            Dg[ci][i] += Fq[q] * dot3(gx[q][i], cD);
+          }
+        }
+      }
     /* the nine terms in .pro order: (x,x),(x,y),(x,z),(y,x),... */
     for(ci = 0; ci < 3; ci++)
       for(cj = 0; cj < 3; cj++) {
@@ -483,6 +567,13 @@ int64_t oracle_assemble_tet10_elasticity(int ne, const double *nodes,
         for(i = 0; i < 10; i++)
           for(j = 0; j < 10; j++) {
             int r = dof[10 * ci + i], c = dof[10 * cj + j];
+            if(r >= 0 && c < 0 && g_fix) {
+              double sc = g_babs ? fabs(g_fix[-c - 1]) * sqrt(fabs(Dg[ci][i] * Dg[cj][j])) : 0.;
+              if(Ek[i][j])
+                badd_scaled(b, r, (g_fix[-c - 1] * 1.) * -Ek[i][j], sc);
+              else
+                bscale(r, sc);
+            }
             if(r < 0 || c < 0) continue;
             coo_add(&m, r, c, Ek[i][j]);
           }

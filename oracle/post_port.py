@@ -21,10 +21,18 @@ CURL_EDGE = np.array([[0., -2., 2.], [2., 0., -2.], [-2., 2., 0.],
 
 
 def _dof_values(dm, x, nh):
+    """Per element and local DOF the field coefficient of each harmonic:
+    the unknown's value, or a fixed DOF's value (dm.fixed_values; 0 when the
+    fixed DOFs are homogeneous)."""
     ed = dm.elem_dofs
+    fv = getattr(dm, "fixed_values", None)
     vals = np.zeros(ed.shape + (nh,))
     for h in range(nh):
-        vals[..., h] = np.where(ed >= 0, x[np.maximum(ed, 0) + h], 0.0)
+        fixed = 0.0
+        if fv is not None:
+            f = np.asarray(fv, np.float64).reshape(len(fv), -1)
+            fixed = f[np.maximum(-ed - 1, 0), h]
+        vals[..., h] = np.where(ed >= 0, x[np.maximum(ed, 0) + h], fixed)
     return vals
 
 

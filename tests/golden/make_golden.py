@@ -60,6 +60,16 @@ CASES = [
     ("eddy_n8", W.eddy_2d, dict(n=8, seed=41, freq=500.0),
      dict(Algorithm=8, Preconditioner=6, Krylov_Size=50, Stopping_Test=1e-10,
           Nb_Iter_Max=2000, Renumbering_Technique=1)),
+    # non-homogeneous Dirichlet values (workloads.DIRICHLET_SETS)
+    ("ms2d_n12_dir", W.magnetostatics_2d, dict(n=12, seed=13, dirichlet=1),
+     dict(Algorithm=8, Preconditioner=6, Krylov_Size=50, Stopping_Test=1e-12,
+          Nb_Iter_Max=2000, Renumbering_Technique=1)),
+    ("el_p2_n2_dir", W.elasticity_p2, dict(n=2, seed=23, dirichlet=2),
+     dict(Algorithm=1, Preconditioner=0, Scaling=1, Stopping_Test=1e-10,
+          Nb_Iter_Max=5000, Renumbering_Technique=1)),
+    ("eddy_n8_dir", W.eddy_2d, dict(n=8, seed=42, freq=500.0, dirichlet=1),
+     dict(Algorithm=8, Preconditioner=6, Krylov_Size=50, Stopping_Test=1e-10,
+          Nb_Iter_Max=2000, Renumbering_Technique=1)),
 ]
 
 

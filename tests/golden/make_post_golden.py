@@ -30,6 +30,9 @@ CASES = [
     ("post_ms2d_n8", W.magnetostatics_2d, dict(n=8, seed=11), 2),
     ("post_eddy_n8", W.eddy_2d, dict(n=8, seed=41, freq=500.0), 2),
     ("post_cc_edge_n4", W.curlcurl_edge, dict(n=4, seed=31), 3),
+    # fixed DOFs with values (workloads.DIRICHLET_SETS)
+    ("post_ms2d_n8_dir", W.magnetostatics_2d, dict(n=8, seed=14, dirichlet=1), 2),
+    ("post_eddy_n8_dir", W.eddy_2d, dict(n=8, seed=43, freq=500.0, dirichlet=1), 2),
 ]
 PAR = "Algorithm 8\nPreconditioner 6\nKrylov_Size 50\nStopping_Test 1e-12\n" \
       "Nb_Iter_Max 5000\n"

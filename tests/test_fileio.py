@@ -116,3 +116,45 @@ def test_reference_post_processing_reads_our_res(binary):
         assert np.array_equal(got, d["elem_vals"])
     else:  # the solution went through %.16g
         assert np.abs(got - d["elem_vals"]).max() <= 1e-14 * np.abs(d["elem_vals"]).max()
+
+
+@pytest.mark.skipif(not os.path.exists(REF), reason="reference binary not built")
+@pytest.mark.parametrize("gen,kw", [
+    (W.magnetostatics_2d, dict(n=6, seed=3)),
+    (W.magnetostatics_2d, dict(n=5, seed=1, dirichlet=1)),
+    (W.eddy_2d, dict(n=4, seed=4, freq=500.0, dirichlet=1)),
+    (W.elasticity_p2, dict(n=2, seed=21)),
+    (W.elasticity_p2, dict(n=2, seed=23, dirichlet=2)),
+    (W.curlcurl_edge, dict(n=3, seed=31)),
+], ids=["ms2d", "ms2d_dir", "eddy_dir", "el_p2", "el_p2_dir", "cc_edge"])
+def test_pre_writer_matches_reference_bytes(gen, kw, tmp_path):
+    # the reference writes its .pre at pre-processing; ours from the DofMap
+    p = gen(**kw)
+    dm = W.dofmap_for(p)
+    W.write_pro(p, str(tmp_path / "p.pro"))
+    W.write_msh22(p.mesh, str(tmp_path / "p.msh"))
+    r = subprocess.run([REF, "p.pro", "-pre", "R", "-msh", "p.msh", "-v", "1"], cwd=tmp_path,
+                       stdin=subprocess.DEVNULL, capture_output=True, text=True, timeout=300)
+    assert (tmp_path / "p.pre").exists(), r.stdout[-2000:] + r.stderr[-2000:]
+    FIO.write_pre(str(tmp_path / "ours.pre"), p.mesh, dm)
+    assert (tmp_path / "ours.pre").read_bytes() == (tmp_path / "p.pre").read_bytes()
+
+
+def test_pre_writer_round_trips_the_numbering(tmp_path):
+    # parsed back, the records give every element's unknown numbers
+    p = W.elasticity_p2(n=3, seed=2)
+    dm = W.dofmap_for(p)
+    FIO.write_pre(str(tmp_path / "p.pre"), p.mesh, dm)
+    lines = (tmp_path / "p.pre").read_text().splitlines()
+    nrec, nunk = map(int, lines[8].split())
+    assert nunk == dm.n_dof
+    num = {}
+    for l in lines[9:9 + nrec]:
+        t = l.split()
+        if t[3] == "1":
+            num[(int(t[0]), int(t[1]))] = int(t[4]) - 1
+    nv = p.mesh.elems.shape[1]
+    for k in range(30):
+        key = [(k // nv + 1, int(v) + 1) for v in p.mesh.elems[:, k % nv]]
+        got = np.array([num.get(kk, -1) for kk in key])
+        assert np.array_equal(got, np.where(dm.elem_dofs[:, k] >= 0, dm.elem_dofs[:, k], -1))

@@ -579,3 +579,39 @@ def test_tiny_systems_match_oracle(n, algorithm, precond):
                                   nb_iter_max=100, stopping_test=float(np.float32(1e-10)))
     assert info["status"] == st and info["iterations"] == its, (info, st, its)
     assert np.linalg.norm(x.numpy() - xo) <= 1e-12 * np.linalg.norm(xo)
+
+
+@pytest.mark.parametrize("renumbering", [0, 1])
+@pytest.mark.parametrize("algorithm", [8, 9])
+def test_solve_again_reuses_the_factorisation(renumbering, algorithm):
+    # LinAlg_SolveAgain keeps the ILU(0) factor of the previous solve of A
+    # (Re_Use_LU, LinAlg_SPARSKIT.cpp:578-585): a second right-hand side is
+    # solved without factoring again, with the same iterates as a solve that
+    # factors; a Generate makes a new matrix, whose first solve factors
+    p = W.magnetostatics_2d(24, seed=12)
+    dm = W.dofmap_for(p)
+    par = {"Algorithm": algorithm, "Preconditioner": 6, "Krylov_Size": 50,
+           "Renumbering_Technique": renumbering, "Stopping_Test": "1e-12"}
+    S = _solver(par)
+    n = dm.n_dof
+    A, b = G_.generate_problem(p, dm)
+    x = LA.LinAlg_CreateVector(None, n)
+    info0 = LA.LinAlg_Solve(A, b, S, x)
+    assert info0["status"] == 0 and info0["ilu_factorized"] == 1
+    b2 = LA.LinAlg_CreateVector(None, n)
+    b2.set(b.numpy() * 0.5 + 1e-3 * np.cos(np.arange(n)))
+    xa = LA.LinAlg_CreateVector(None, n)
+    ia = LA.LinAlg_SolveAgain(A, b2, S, xa)
+    assert ia["status"] == 0 and ia["ilu_factorized"] == 0
+    assert S["re_use_lu"] == 0  # restored after the call
+    xf = LA.LinAlg_CreateVector(None, n)
+    fresh = LA.LinAlg_Solve(A, b2, S, xf)
+    assert fresh["ilu_factorized"] == 1
+    # the same factor either way: the same iterates
+    assert ia["iterations"] == fresh["iterations"]
+    assert np.array_equal(xa.numpy(), xf.numpy())
+    # after a Generate: a new matrix, factored on its first solve
+    G_.generate(A, b, G_.host_batch(G_.term_arrays(p, dm)), pattern=True)
+    xg = LA.LinAlg_CreateVector(None, n)
+    ig = LA.LinAlg_SolveAgain(A, b, S, xg)
+    assert ig["status"] == 0 and ig["ilu_factorized"] == 1

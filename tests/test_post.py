@@ -15,7 +15,9 @@ from oracle import post_port as PP
 from tests.golden_cases import GOLDEN
 
 CASES = {"post_ms2d_n8": W.magnetostatics_2d, "post_eddy_n8": W.eddy_2d,
-         "post_cc_edge_n4": W.curlcurl_edge}
+         "post_cc_edge_n4": W.curlcurl_edge,
+         # fixed DOFs with non-zero values enter {a} and {d a}
+         "post_ms2d_n8_dir": W.magnetostatics_2d, "post_eddy_n8_dir": W.eddy_2d}
 
 
 def load(name):

@@ -25,10 +25,13 @@ def our_records(p, dm):
     tables touch."""
     m = p.mesh
     f = p.formulation
+    # a fixed DOF is -1 in the .pre comparison (with Dirichlet values the
+    # tables number fixed DOFs -1-k)
+    edofs = np.where(dm.elem_dofs >= 0, dm.elem_dofs, -1)
     if f in ("magnetostatics2d", "nonlinear2d", "eddy2d"):
         ent = m.elems + 1
         nt = np.ones_like(ent)
-        d = dm.elem_dofs
+        d = edofs
         recs = [np.stack([nt.ravel(), ent.ravel(), np.zeros(ent.size, np.int64),
                           d.ravel()], 1)]
         if f == "eddy2d":
@@ -41,7 +44,7 @@ def our_records(p, dm):
         ent = np.tile(m.elems + 1, (1, 3))
         nt = np.repeat(np.arange(1, 4), nv)[None, :].repeat(m.n_elems, 0)
         r = np.stack([nt.ravel(), ent.ravel(), np.zeros(ent.size, np.int64),
-                      dm.elem_dofs.ravel()], 1)
+                      edofs.ravel()], 1)
     elif f == "curlcurl":
         ve = m.elems[:, W.TET4_EDGES].reshape(-1, 2)
         nn = m.n_nodes
@@ -50,7 +53,7 @@ def our_records(p, dm):
         order = np.argsort(ekey)
         ent = order[np.searchsorted(ekey[order], key)] + 1
         r = np.stack([np.ones(len(ent), np.int64), ent, np.zeros(len(ent), np.int64),
-                      dm.elem_dofs.ravel()], 1)
+                      edofs.ravel()], 1)
     else:
         raise ValueError(f)
     return np.unique(r.astype(np.int64), axis=0)

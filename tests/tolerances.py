@@ -22,7 +22,12 @@ unknown's 2 x 2 diagonal block, |A_ii| + |A_i,i^1|) and sum |t_k| the
 entry's sum of |element contribution| from the oracle's element loop.  It
 means: entries agree to 1e-12 relative, or to 1e-13 of the Jacobi-scaled
 matrix D^-1/2 A D^-1/2 that the solvers iterate on.  RHS entries use the
-sum of |element contribution| to the row.
+oracle's first-order rounding scale of the row (oracle.assemble(...,
+with_abs=True)): the sum of |element contribution|, for an eliminated fixed
+value |g_j| sqrt(Ek_ii Ek_jj), and for the nonlinear terms evaluated at a
+field b = sum_i a_i curl N_i the field's own rounding (the nodal values
+cancel in the curl) times the B-H law's sensitivity 1 + 2 |b|^2 / b_sat^2;
+1e-13 is about 450 units in the last place of that scale.
 """
 import numpy as np
 
