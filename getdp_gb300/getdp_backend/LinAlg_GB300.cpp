@@ -17,6 +17,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <set>
+
 #include "DofData.h"
 #include "GetDPConfig.h"
 #include "LinAlg.h"
@@ -69,6 +71,14 @@ static void dev(gVector *V)
     V->state = BOTH;
   }
 }
+
+// matrices something has been added to since they were created or zeroed
+// (the Generate hook, Generate_GB300.cpp, takes only an untouched matrix)
+static std::set<gb300_matrix *> g_touched;
+static void touched(gMatrix *M) { g_touched.insert(M->M); }
+int GB300_MatrixUntouched(gMatrix *M) { return M->M && !g_touched.count(M->M); }
+void GB300_VectorOnDevice(gVector *V) { dev(V); }
+void GB300_VectorDeviceWritten(gVector *V) { V->state = DEV; }
 
 void LinAlg_InitializeSolver(int *sargc, char ***sargv)
 {
@@ -156,6 +166,7 @@ void LinAlg_CreateVector(gVector *V, gSolver *Solver, int n)
 void LinAlg_CreateMatrix(gMatrix *M, gSolver *Solver, int n, int m)
 {
   ok(gb300_matrix_create(ctx(), n, &M->M));
+  g_touched.erase(M->M);
 }
 
 void LinAlg_DestroySolver(gSolver *Solver) {}
@@ -169,6 +180,7 @@ void LinAlg_DestroyVector(gVector *V)
 
 void LinAlg_DestroyMatrix(gMatrix *M)
 {
+  g_touched.erase(M->M);
   gb300_matrix_destroy(M->M);
   M->M = nullptr;
 }
@@ -210,7 +222,11 @@ void LinAlg_ZeroVector(gVector *V)
   V->state = HOST;
 }
 
-void LinAlg_ZeroMatrix(gMatrix *M) { ok(gb300_matrix_zero(M->M)); }
+void LinAlg_ZeroMatrix(gMatrix *M)
+{
+  ok(gb300_matrix_zero(M->M));
+  g_touched.erase(M->M);
+}
 
 void LinAlg_ScanScalar(FILE *file, gScalar *S) { fscanf(file, "%lf", &S->s); }
 
@@ -489,12 +505,14 @@ void LinAlg_AddDoubleInMatrix(double d, gMatrix *M, int i, int j)
   int *DummyDof;
   if((DummyDof = Current.DofData->DummyDof))
     if((DummyDof[i] == 1 || DummyDof[j] == 1) && (i != j)) return;
+  touched(M);
   ok(gb300_matrix_add_double(M->M, d, i, j));
 }
 
 void LinAlg_AddComplexInMatrix(double d1, double d2, gMatrix *M, int i, int j,
                                int k, int l)
 {
+  touched(M);
   ok(gb300_matrix_add_complex(M->M, d1, d2, i, j, k, l));
 }
 
@@ -547,6 +565,7 @@ static void add_scaled(gMatrix *M1, gMatrix *M2, double d)
       ri[k] = i;
       v[k] *= d;
     }
+  touched(M1);
   ok(gb300_matrix_add_coo(M1->M, nnz, ri, ci, v));
   Free(rp);
   Free(ci);
