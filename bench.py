@@ -428,7 +428,7 @@ def run_other(args, ws, rank, local):
         t_asm = time.perf_counter() - t0
         # the reference solves with RCMK renumbering (its default); one solve
         # capped at a bounded number of iterations, extrapolated
-        cap = 200 if args.workload == "curlcurl" else 5000
+        cap = 600 if args.workload == "curlcurl" else 5000
         t0 = time.perf_counter()
         xs, st_, its, r_ = oracle.solve(ip, ix, dv, bb, algorithm=par["Algorithm"],
                                         preconditioner=6, renumbering=1,
