@@ -127,6 +127,8 @@ SIGNATURES = {
     "gb300_msh_group": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_LL),
                              ctypes.POINTER(_I), ctypes.POINTER(_I), _PP, _PP, _PP]),
     "gb300_matrix_set_correction": (_I, [_P, _P, _I]),
+    "gb300_matrix_set_aggregates": (_I, [_P, _P, _I]),
+    "gb300_matrix_coarse_energy": (_I, [_P, _P, _P]),
     "gb300_matrix_scale_correction": (_I, [_P, ctypes.c_double]),
     "gb300_precond_apply": (_I, [_P, ctypes.POINTER(SolverParams), _P, _P]),
     "gb300_mpnn_param_count": (_I, []),
@@ -137,6 +139,7 @@ SIGNATURES = {
     "gb300_mpnn_infer": (_I, [_P, _P]),
     "gb300_mpnn_loss_grad": (_I, [_P, _P, _P, _P, _I, ctypes.POINTER(_D), _P]),
     "gb300_mpnn_adam_step": (_I, [_P, ctypes.c_float, ctypes.c_float]),
+    "gb300_mpnn_set_loss": (_I, [_P, _I]),
     "gb300_post_elements": (_I, [ctypes.POINTER(TermBatch), _P, _P]),
     "gb300_post_points": (_I, [ctypes.POINTER(TermBatch), _P, _I, _P, _P, _P, _P]),
     "gb300_solve_batch": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, _I,

@@ -1100,6 +1100,7 @@ int generate_pattern(gb300_matrix *A, const gb300_term_batch *t)
       }
       if(A->nnz > 0) GB_CUDA(cudaMemsetAsync(A->val.p, 0, sizeof(double) * A->nnz, st));
       A->val32_valid = false;
+      gb::coarse_values_changed(A);
       A->block3 = G->block3;
       A->node_blocks = G->node_blocks;
       A->block_rows = G->block_rows;
@@ -1672,6 +1673,7 @@ int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t,
     return GB300_ERR_ARG;
   }
   A->val32_valid = false;
+  gb::coarse_values_changed(A);
   return GB300_OK;
 }
 

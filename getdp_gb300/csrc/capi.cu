@@ -431,6 +431,7 @@ int gb300_matrix_destroy(gb300_matrix *A)
   cudaStreamSynchronize(A->ctx->stream);
   if(A->ilu) ilu_free(A->ilu);
   colour_free(A->mc);
+  coarse_free(A->coarse);
   delete A;
   return GB300_OK;
 }
@@ -443,6 +444,7 @@ int gb300_matrix_reset(gb300_matrix *A)
   A->hv.clear();
   A->csr_valid = false;
   A->val32_valid = false;
+  gb::coarse_values_changed(A);
   A->nnz = 0;
   A->block_rows = 1;
   if(A->ilu) {
@@ -571,6 +573,7 @@ int gb300_matrix_zero(gb300_matrix *A)
     GB_TRY(gb300_matrix_assemble(A));
   }
   A->val32_valid = false;
+  gb::coarse_values_changed(A);
   return GB300_OK;
 }
 
@@ -635,6 +638,7 @@ int gb300_matrix_set_csr(gb300_matrix *A, long long nnz, const int *rowptr,
   A->csr_valid = true;
   A->pattern_version++;
   A->val32_valid = false;
+  gb::coarse_values_changed(A);
   A->block3 = false;
   A->node_blocks = false;
   A->bsr_var32 = A->bsr_var64 = -1;
@@ -873,6 +877,37 @@ int gb300_matrix_set_correction(gb300_matrix *A, const double *values, int on_de
     GB_CUDA(cudaStreamSynchronize(A->ctx->stream));
   }
   A->corr_version = A->pattern_version;
+  return GB300_OK;
+}
+
+int gb300_matrix_set_aggregates(gb300_matrix *A, const int *agg, int n_agg)
+{
+  GB_TRY(check(A, "matrix"));
+  GB_TRY(gb300_matrix_assemble(A));
+  if(A->n > 0) GB_TRY(check(agg, "aggregates"));
+  return coarse_set(A, agg, n_agg);
+}
+
+int gb300_matrix_coarse_energy(gb300_matrix *A, const gb300_vector *u, double *ucu)
+{
+  GB_TRY(check(A, "matrix"));
+  GB_TRY(check(u, "vector"));
+  GB_TRY(check(ucu, "result"));
+  GB_TRY(gb300_matrix_assemble(A));
+  if(u->n != A->n) {
+    set_error("coarse energy: vector size %d, matrix size %d", u->n, A->n);
+    return GB300_ERR_ARG;
+  }
+  if(!coarse_valid(A)) {
+    set_error("coarse energy: the matrix has no aggregates on its current pattern");
+    return GB300_ERR_ARG;
+  }
+  cudaStream_t st = A->ctx->stream;
+  DevBuf<double> d;
+  GB_TRY(d.alloc(1));
+  GB_TRY(coarse_energy(A, u->d.p, d.p, st));
+  GB_CUDA(cudaMemcpyAsync(ucu, d.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
   return GB300_OK;
 }
 

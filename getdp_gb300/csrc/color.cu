@@ -230,6 +230,7 @@ void colour_free(Colouring *c)
   if(!c) return;
   if(c->B) {
     if(c->B->ilu) ilu_free(c->B->ilu);
+    coarse_free(c->B->coarse);
     delete c->B;
   }
   delete c;
@@ -393,6 +394,7 @@ int gmres_solve_coloured(gb300_matrix *A, const double *val, const double *rhs,
                                                           B->corr.p);
     B->corr_version = B->pattern_version;
   }
+  if(coarse_valid(A)) GB_TRY(coarse_follow(A, B, C, st));  // the aggregates too
   GB_CUDA(cudaGetLastError());
   rc = gmres_solve(B, B->val.p, rb.p, yb.p, p, info, W);
   if(rc != GB300_OK) return rc;
@@ -409,8 +411,11 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
 {
   cudaStream_t st = A->ctx->stream;
   const int n = A->n;
-  const bool learned = (p->preconditioner == kPrecondLearned);
-  if(p->preconditioner != 6 && !learned) {
+  const bool learned = (p->preconditioner == kPrecondLearned ||
+                        p->preconditioner == kPrecondLearnedCoarse);
+  const bool coarse = (p->preconditioner == kPrecondCoarse ||
+                       p->preconditioner == kPrecondLearnedCoarse);
+  if(p->preconditioner != 6 && !learned && !coarse) {
     set_error("preconditioner apply: Preconditioner %d is not an ILU(0)", p->preconditioner);
     return GB300_ERR_UNSUPPORTED;
   }
@@ -418,12 +423,20 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
     set_error("Preconditioner %d needs a correction on the matrix pattern", p->preconditioner);
     return GB300_ERR_ARG;
   }
+  if(coarse && !coarse_valid(A)) {
+    set_error("Preconditioner %d needs aggregates on the matrix pattern", p->preconditioner);
+    return GB300_ERR_ARG;
+  }
   const bool fp32 = (p->precision != 0);
   gb300_matrix *M = A;
-  DevBuf<double> vb, zb, t1, t2;
+  DevBuf<double> vb, zb, t1, t2, t3, t4;
   DevBuf<float> t32;
   GB_TRY(t1.alloc(n));
   GB_TRY(t2.alloc(n));
+  if(coarse) {
+    GB_TRY(t3.alloc(n));
+    GB_TRY(t4.alloc(n));
+  }
   if(fp32) GB_TRY(t32.alloc(n));
   const double *vin = v;
   double *zout = z;
@@ -444,6 +457,7 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
                                                               M->corr.p);
         M->corr_version = M->pattern_version;
       }
+      if(coarse) GB_TRY(coarse_follow(A, M, C, st));
       vin = vb.p;
       zout = zb.p;
     }
@@ -454,8 +468,16 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
     set_error("Zero pivot on line %d in ILU", zr);
     return GB300_ERR_ZERO_PIVOT;
   }
-  ilu_apply(M, fp32, vin, zout, fp32 ? t32.p : nullptr, nullptr, st);
-  if(learned) correction_apply(M, M->val.p, vin, zout, t1.p, t2.p, nullptr, st);
+  auto smooth = [&](const double *vv, double *zz) {
+    ilu_apply(M, fp32, vv, zz, fp32 ? t32.p : nullptr, nullptr, st);
+    if(learned) correction_apply(M, M->val.p, vv, zz, t1.p, t2.p, nullptr, st);
+  };
+  if(coarse) {
+    GB_TRY(coarse_setup(M, M->val.p, false));
+    two_level_apply(M, M->val.p, vin, zout, t3.p, t4.p, nullptr, st, smooth);
+  }
+  else
+    smooth(vin, zout);
   if(C) unpermute_solution(C, zout, z, st);
   GB_CUDA(cudaGetLastError());
   GB_CUDA(cudaStreamSynchronize(st));

@@ -16,6 +16,9 @@ namespace gb {
 
 struct ilu_data;
 struct Colouring;
+struct Coarse;
+// A's values changed: a coarse inverse made from the old ones is stale
+void coarse_values_changed(gb300_matrix *A);
 
 // last error message, per thread (read through gb300_last_error)
 void set_error(const char *fmt, ...);
@@ -313,6 +316,9 @@ struct gb300_matrix {
   // corr_version == pattern_version)
   gb::DevBuf<double> corr;
   unsigned corr_version = ~0u;
+  // aggregates and coarse operator of the two-level preconditioners
+  // (gb300_matrix_set_aggregates; valid while their version is pattern_version)
+  gb::Coarse *coarse = nullptr;
   // the pattern came from the context's Generate cache entry gen_tag while
   // pattern_version was gen_pv (a later change of the pattern bumps the
   // version and so invalidates the link)

@@ -982,17 +982,26 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
     set_error("Krylov_Size %d exceeds this backend's maximum %d", m, kMaxKrylov);
     return GB300_ERR_UNSUPPORTED;
   }
-  // 20: ILU(0) followed by the learned correction on A's pattern
-  const bool learned = (p->preconditioner == kPrecondLearned);
-  bool precond = (p->preconditioner == 6) || learned;
+  // 20: ILU(0) followed by the learned correction on A's pattern; 21, 22:
+  // the two-level cycle on aggregates around ILU(0) (22: and the correction)
+  const bool learned = (p->preconditioner == kPrecondLearned ||
+                        p->preconditioner == kPrecondLearnedCoarse);
+  const bool coarse = (p->preconditioner == kPrecondCoarse ||
+                       p->preconditioner == kPrecondLearnedCoarse);
+  bool precond = (p->preconditioner == 6) || learned || coarse;
   if(p->preconditioner != 0 && p->preconditioner != 6 && p->preconditioner != 8 &&
-     !learned) {
+     !learned && !coarse) {
     set_error("Preconditioner %d is not supported by this backend", p->preconditioner);
     return GB300_ERR_UNSUPPORTED;
   }
   if(learned && !correction_valid(A)) {
     set_error("Preconditioner %d needs a correction on the matrix pattern "
               "(gb300_matrix_set_correction)", p->preconditioner);
+    return GB300_ERR_ARG;
+  }
+  if(coarse && !coarse_valid(A)) {
+    set_error("Preconditioner %d needs aggregates on the matrix pattern "
+              "(gb300_matrix_set_aggregates)", p->preconditioner);
     return GB300_ERR_ARG;
   }
   bool fp32 = (p->precision != 0);
@@ -1006,6 +1015,7 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
       return GB300_ERR_ZERO_PIVOT;
     }
   }
+  if(coarse) GB_TRY(coarse_setup(A, val, p->re_use_lu != 0));
   size_t ldv = (size_t)n;
   double *V = (double *)W.vec(0, sizeof(double) * ldv * (m + 1));
   double *Z = flexible ? (double *)W.vec(1, sizeof(double) * ldv * m) : nullptr;
@@ -1019,8 +1029,10 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   int *okflag = (int *)W.vec(7, sizeof(int));
   double *t1 = learned ? (double *)W.vec(8, sizeof(double) * n) : nullptr;
   double *t2 = learned ? (double *)W.vec(9, sizeof(double) * n) : nullptr;
+  double *t3 = coarse ? (double *)W.vec(13, sizeof(double) * n) : nullptr;
+  double *t4 = coarse ? (double *)W.vec(14, sizeof(double) * n) : nullptr;
   if(!V || (flexible && !Z) || !r || !u || !zt || (fp32 && !t32) || !part || !pn || !S ||
-     (learned && (!t1 || !t2)))
+     (learned && (!t1 || !t2)) || (coarse && (!t3 || !t4)))
     return GB300_ERR_CUDA;
   GmState h0;
   memset(&h0, 0, sizeof(h0));
@@ -1037,12 +1049,20 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   // one per 2048 rows up to kReduceBlocks (small systems keep the
   // one-block reductions short); fixed for a given n, so deterministic
   const int nb = std::min(kReduceBlocks, std::max(152, (n + 2047) / 2048));
-  auto precond_apply = [&](const double *v, double *z, const int *flag) {
+  auto smooth = [&](const double *v, double *z, const int *flag) {
     if(precond)
       ilu_apply(A, fp32, v, z, t32, flag, st);
     else
       k_cvt<double, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, z, flag);
     if(learned) correction_apply(A, val, v, z, t1, t2, flag, st);
+  };
+  auto precond_apply = [&](const double *v, double *z, const int *flag) {
+    if(!coarse) {
+      smooth(v, z, flag);
+      return;
+    }
+    two_level_apply(A, val, v, z, t3, t4, flag, st,
+                    [&](const double *vv, double *zz) { smooth(vv, zz, flag); });
   };
 
   cudaGraph_t graph;

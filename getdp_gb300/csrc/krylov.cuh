@@ -1,6 +1,8 @@
 // Solver-internal declarations (work space, ILU(0), GMRES).
 #pragma once
 
+#include <functional>
+
 #include <cstring>
 
 #include "sparse.cuh"
@@ -62,6 +64,45 @@ int bsr_check(const Bsr3 &B, cudaStream_t st);
 // Preconditioner 20 (not a Sparskit value): ILU(0), then z += G (v - A z)
 // with G the learned correction on A's pattern (gb300_matrix_set_correction)
 constexpr int kPrecondLearned = 20;
+// Preconditioners 21 and 22 (not Sparskit values): the two-level cycle
+// z = S v; z += P0 Ac^-1 P0^T (v - A z); z += S (v - A z) on the aggregates
+// of gb300_matrix_set_aggregates, with S = ILU(0) (21) or ILU(0) followed by
+// the learned correction (22) (coarse.cu)
+constexpr int kPrecondCoarse = 21;
+constexpr int kPrecondLearnedCoarse = 22;
+constexpr int kMaxCoarse = 2048;  // dense coarse inverse: at most 32 MiB
+struct Coarse {
+  int n = 0, nc = 0;
+  unsigned version = ~0u;   // the owner's pattern_version when set
+  unsigned stamp = 0;       // bumped by every new set of aggregates
+  unsigned followed = ~0u;  // on a permuted copy: the source's stamp it follows
+  int headroom = 0;         // bits kept free in the fixed-point sums
+  bool ready = false;       // inv holds the inverse for the last values
+  DevBuf<int> agg, aperm, aptr;   // aggregate of each row; rows by aggregate
+  DevBuf<double> inv;             // nc x nc, row-major
+  DevBuf<double> rbuf, cbuf;      // Gauss-Jordan pivot rows and columns
+  DevBuf<double> rc, ec;          // coarse residual and correction
+  DevBuf<int> err;
+  DevBuf<double> amax;
+};
+void coarse_free(Coarse *c);
+bool coarse_valid(const gb300_matrix *A);
+int coarse_set(gb300_matrix *A, const int *agg, int nc);
+int coarse_follow(const gb300_matrix *A, gb300_matrix *B, const Colouring *C,
+                  cudaStream_t st);
+int coarse_setup(gb300_matrix *A, const double *val, bool reuse);
+void coarse_correct(const gb300_matrix *A, const double *val, const double *v, double *z,
+                    double *t, const int *flag, cudaStream_t st);
+// w <- (I - A C) w and *wcw = w^T C w (device scalar), C = P0 Ac^-1 P0^T on
+// A's own values (the coarse inverse made once and then reused; t, q: n
+// doubles of scratch) -- the two-level form of the learned correction's loss
+int coarse_energy_project(gb300_matrix *A, double *w, double *t, double *q, double *wcw,
+                          cudaStream_t st);
+// *ucu_dev = u^T C u (same coarse inverse as coarse_energy_project)
+int coarse_energy(gb300_matrix *A, const double *u, double *ucu_dev, cudaStream_t st);
+void two_level_apply(const gb300_matrix *A, const double *val, const double *v, double *z,
+                     double *t3, double *t4, const int *flag, cudaStream_t st,
+                     const std::function<void(const double *, double *)> &smooth);
 bool correction_valid(const gb300_matrix *A);
 void correction_apply(const gb300_matrix *A, const double *val, const double *v,
                       double *z, double *t1, double *t2, const int *flag, cudaStream_t st);

@@ -76,6 +76,7 @@ struct gb300_mpnn {
   gb::DevBuf<float> wq;      // BF16-rounded copy used by the kernels
   gb::DevBuf<float> grad, am, av;  // gradient, Adam moments
   int step = 0;
+  int loss_mode = 0;  // 0: one-level energy loss; 1: after the coarse correction
   gb::MpnnGraph g;
 };
 
@@ -466,19 +467,24 @@ static int mp_forward(gb300_mpnn *net, const gb300_matrix *A)
   return GB300_OK;
 }
 
-static int mp_loss_backward(gb300_mpnn *net, const gb300_matrix *A, const double *r1,
+static int mp_loss_backward(gb300_mpnn *net, gb300_matrix *A, const double *r1,
                             const double *e1, double *loss)
 {
   MpnnGraph &g = net->g;
   cudaStream_t st = A->ctx->stream;
   const int n = A->n;
-  DevBuf<double> y, w, part, ee;
+  const bool two = (net->loss_mode == 1);
+  DevBuf<double> y, w, part, ee, t, q;
   DevBuf<float> dg;
   GB_TRY(y.alloc(n));
   GB_TRY(w.alloc(n));
   GB_TRY(part.alloc(kReduceBlocks));
   GB_TRY(dg.alloc(A->nnz));
-  GB_TRY(ee.alloc(3));
+  GB_TRY(ee.alloc(4));
+  if(two) {
+    GB_TRY(t.alloc(n));
+    GB_TRY(q.alloc(n));
+  }
   // S = e1^T A e1 (solution known), else r1^T D^-1 r1
   if(e1) {
     spmv_plain(A, A->val.p, e1, w.p, st);
@@ -494,8 +500,13 @@ static int mp_loss_backward(gb300_mpnn *net, const gb300_matrix *A, const double
   dot_part64(n, y.p, w.p, part.p, st);
   sum_partials(part.p, ee.p + 2, st);
   k_mp_sub<<<grid_for(n, 256), 256, 0, st>>>(n, r1, w.p);
-  double he[3] = {0., 0., 0.};
-  GB_CUDA(cudaMemcpyAsync(he, ee.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  // two-level loss: the error left after the coarse correction,
+  // (e1 - y)^T (A - A C A) (e1 - y), whose gradient in y is 2 (I - A C) w
+  // with w = A y - r1; w^T C w is what the coarse correction removes
+  GB_CUDA(cudaMemsetAsync(ee.p + 3, 0, sizeof(double), st));
+  if(two) GB_TRY(coarse_energy_project(A, w.p, t.p, q.p, ee.p + 3, st));
+  double he[4] = {0., 0., 0., 0.};
+  GB_CUDA(cudaMemcpyAsync(he, ee.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));
   const double S = he[0];
   if(!(S > 0.)) {
@@ -503,7 +514,7 @@ static int mp_loss_backward(gb300_mpnn *net, const gb300_matrix *A, const double
               "positive definite)");
     return GB300_ERR_ARG;
   }
-  const double hl = S + he[2] - 2. * he[1];  // (relative) energy error x S
+  const double hl = S + he[2] - 2. * he[1] - he[3];  // (relative) energy error x S
   const double E = S;
   // dL/dG_ij = 2 (A y - r1)_i r1_j / S
   k_mp_dg<<<grid_for(n, 256), 256, 0, st>>>(n, A->rowptr.p, A->col.p, g.dscale.p, w.p, r1,
@@ -649,6 +660,11 @@ int gb300_mpnn_loss_grad(gb300_mpnn *net, gb300_matrix *A, const gb300_vector *r
   }
   cudaStream_t st = A->ctx->stream;
   if(!accumulate) GB_CUDA(cudaMemsetAsync(net->grad.p, 0, sizeof(float) * kParams, st));
+  if(net->loss_mode == 1 && !coarse_valid(A)) {
+    set_error("network: the two-level loss needs aggregates on the matrix "
+              "(gb300_matrix_set_aggregates)");
+    return GB300_ERR_ARG;
+  }
   GB_TRY(mp_prepare(net, A));
   GB_TRY(mp_forward(net, A));
   GB_TRY(mp_loss_backward(net, A, r1->d.p, e1 ? e1->d.p : nullptr, loss));
@@ -657,6 +673,16 @@ int gb300_mpnn_loss_grad(gb300_mpnn *net, gb300_matrix *A, const gb300_vector *r
                             cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
   }
+  return GB300_OK;
+}
+
+int gb300_mpnn_set_loss(gb300_mpnn *net, int mode)
+{
+  if(!net || (mode != 0 && mode != 1)) {
+    set_error("network: loss mode must be 0 (one-level) or 1 (two-level)");
+    return GB300_ERR_ARG;
+  }
+  net->loss_mode = mode;
   return GB300_OK;
 }
 

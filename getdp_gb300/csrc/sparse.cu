@@ -300,6 +300,7 @@ int build_pattern_from_elements(gb300_matrix *A, int ne, int nloc,
   A->csr_valid = true;
   A->pattern_version++;
   A->val32_valid = false;
+  gb::coarse_values_changed(A);
   A->block3 = false;
   A->node_blocks = false;
   A->bsr_var32 = A->bsr_var64 = -1;
@@ -459,6 +460,7 @@ int build_csr_from_coo(gb300_matrix *A, long long m, const int *d_r,
   A->csr_valid = true;
   A->pattern_version++;
   A->val32_valid = false;
+  gb::coarse_values_changed(A);
   A->block3 = false;
   A->node_blocks = false;
   A->bsr_var32 = A->bsr_var64 = -1;

@@ -64,6 +64,11 @@ class MPNN:
             g.ctypes.data_as(ctypes.c_void_p) if want_grad else None))
         return loss.value, g
 
+    def set_loss(self, mode: int) -> None:
+        """0: the one-level energy loss; 1: the energy left after the coarse
+        correction of the two-level cycle (the matrices need aggregates)."""
+        check(self.L.gb300_mpnn_set_loss(self.h, int(mode)))
+
     def adam_step(self, lr: float, grad_scale: float = 1.0) -> None:
         check(self.L.gb300_mpnn_adam_step(self.h, ctypes.c_float(lr),
                                           ctypes.c_float(grad_scale)))
@@ -173,6 +178,49 @@ def step_length(A: LA.gMatrix, probes: int = 2, seed: int = 0, renumbering: int 
     return num / den if den > 0 else 0.0
 
 
+def coarse_energy(A: LA.gMatrix, u: LA.gVector) -> float:
+    """u^T C u, C = P0 Ac^-1 P0^T on A's aggregates (its own values)."""
+    out = ctypes.c_double()
+    u._flush()
+    check(_lib.load().gb300_matrix_coarse_energy(A.h, u.h, ctypes.byref(out)))
+    return out.value
+
+
+def step_length_two_level(A: LA.gMatrix, probes: int = 2, seed: int = 0,
+                          renumbering: int = 1, precision: int = 0) -> float:
+    """step_length for the correction inside the two-level cycle: the step
+    w that minimises the energy of the error left after the coarse
+    correction, (e1 - w g)^T (A - A C A) (e1 - w g), over random probes:
+    w = (g.r1 - (Ag)^T C r1) / (g.Ag - (Ag)^T C Ag), the cross term by
+    polarisation, 2 u^T C v = (u+v)^T C (u+v) - u^T C u - v^T C v.  A needs
+    aggregates and the correction."""
+    L = _lib.load()
+    rng = np.random.default_rng(seed)
+    n = A.n
+    S6 = ilu_params(renumbering)
+    S6.set("Precision", precision)
+    S20 = ilu_params(renumbering)
+    S20.set("Preconditioner", 20)
+    S20.set("Precision", precision)
+    v, z1, z2, r1, ag, sm = (LA.gVector(n) for _ in range(6))
+    num = den = 0.0
+    for _ in range(probes):
+        v.set(rng.standard_normal(n))
+        check(L.gb300_precond_apply(A.h, ctypes.byref(S6.params), v.h, z1.h))
+        check(L.gb300_precond_apply(A.h, ctypes.byref(S20.params), v.h, z2.h))
+        check(L.gb300_vector_axpby(-1.0, z1.h, 1.0, z2.h))    # g = z2 - z1
+        check(L.gb300_matrix_mult(A.h, z1.h, r1.h))
+        check(L.gb300_vector_axpby(1.0, v.h, -1.0, r1.h))     # r1 = v - A z1
+        check(L.gb300_matrix_mult(A.h, z2.h, ag.h))           # A g
+        check(L.gb300_vector_axpby(1.0, ag.h, 0.0, sm.h))
+        check(L.gb300_vector_axpby(1.0, r1.h, 1.0, sm.h))     # A g + r1
+        q_ag, q_r, q_s = coarse_energy(A, ag), coarse_energy(A, r1), coarse_energy(A, sm)
+        g, r, a = z2.numpy(), r1.numpy(), ag.numpy()
+        num += float(r @ g) - 0.5 * (q_s - q_ag - q_r)
+        den += float(g @ a) - q_ag
+    return num / den if den > 0 else 0.0
+
+
 def train(net: MPNN, samples: list, epochs: int = 20, lr: float = 3e-3,
           batch: int = 8, seed: int = 0) -> list:
     """Adam on mini-batches of systems; returns the mean loss per epoch."""
@@ -271,6 +319,79 @@ class NewtonSolver:
                 self.failures += 1
         if info["preconditioner"] != "learned":
             self.last_plain = info["iterations"]
+        self.log.append({k: info.get(k) for k in ("preconditioner", "iterations",
+                                                  "learned_attempt_iterations", "step")})
+        return info
+
+
+class TwoLevelNewtonSolver:
+    """The linear solve of each Newton step with the learned correction
+    inside the two-level cycle (Preconditioner 22, FGMRES), as a callable
+    for nonlinear.newton.  The method without the network is the same cycle
+    with plain ILU(0) smoothing (Preconditioner 21): it is used when the
+    energy-optimal step of the correction is below min_step, when the
+    learned solve does not converge within the last plain step count (the
+    first time, first_cap), and for good after max_failures such attempts.
+    The FP64 residual decides in every case."""
+
+    def __init__(self, net: MPNN, agg, n_agg: int, stopping_test: float = 1e-10,
+                 krylov: int = 50, nb_iter_max: int = 20000, precision: int = 1,
+                 first_cap: int = 2000, max_failures: int = 1, min_step: float = 0.05):
+        self.net = net
+        self.agg = np.ascontiguousarray(agg, np.int32)
+        self.n_agg = int(n_agg)
+        self.stop = stopping_test
+        self.krylov = krylov
+        self.nb_iter_max = nb_iter_max
+        self.precision = precision
+        self.first_cap = first_cap
+        self.max_failures = max_failures
+        self.min_step = min_step
+        self.failures = 0
+        self.last_plain = None
+        self.seen = None
+        self.log = []
+
+    def _params(self, prec: int, cap: int) -> LA.gSolver:
+        S = LA.LinAlg_CreateSolver(None)
+        for k, v in dict(Algorithm=9, Preconditioner=prec, Krylov_Size=self.krylov,
+                         Nb_Iter_Max=cap, Renumbering_Technique=1,
+                         Precision=self.precision).items():
+            S.set(k, v)
+        S["stopping_test"] = self.stop
+        return S
+
+    def _plain(self, A, b, x, why: str, extra: dict) -> dict:
+        info = LA.LinAlg_Solve(A, b, self._params(21, self.nb_iter_max), x)
+        info["preconditioner"] = why
+        info.update(extra)
+        self.last_plain = info["iterations"]
+        return info
+
+    def __call__(self, A: LA.gMatrix, b: LA.gVector, x: LA.gVector) -> dict:
+        if self.seen is not A:
+            A.set_aggregates(self.agg, self.n_agg)
+            self.seen = A
+        if self.failures >= self.max_failures:
+            info = self._plain(A, b, x, "two-level ilu0 (learned off)", {})
+        else:
+            self.net.infer(A)
+            omega = step_length_two_level(A, precision=self.precision)
+            if omega < self.min_step:
+                info = self._plain(A, b, x, "two-level ilu0 (correction rejected)",
+                                   dict(step=omega, learned_attempt_iterations=0))
+                self.failures += 1
+            else:
+                check(_lib.load().gb300_matrix_scale_correction(A.h, ctypes.c_double(omega)))
+                cap = self.last_plain if self.last_plain else self.first_cap
+                info = LA.LinAlg_Solve(A, b, self._params(22, cap), x)
+                info["preconditioner"] = "two-level learned"
+                info["step"] = omega
+                if info["status"] != 0:
+                    self.failures += 1
+                    info = self._plain(A, b, x, "two-level ilu0 (fallback)",
+                                       dict(step=omega,
+                                            learned_attempt_iterations=info["iterations"]))
         self.log.append({k: info.get(k) for k in ("preconditioner", "iterations",
                                                   "learned_attempt_iterations", "step")})
         return info

@@ -237,6 +237,14 @@ class gMatrix:
         dv = np.ascontiguousarray(data, np.float64)
         check(_lib.load().gb300_matrix_set_csr(self.h, len(dv), _ptr(ip), _ptr(ix), _ptr(dv)))
 
+    def set_aggregates(self, agg, n_agg: Optional[int] = None) -> None:
+        """Aggregates of the unknowns for the two-level preconditioners
+        (Preconditioner 21, 22): agg[i] in 0 .. n_agg - 1 for every row."""
+        a = np.ascontiguousarray(agg, np.int32)
+        if n_agg is None:
+            n_agg = int(a.max()) + 1 if len(a) else 0
+        check(_lib.load().gb300_matrix_set_aggregates(self.h, _ptr(a), int(n_agg)))
+
     def add_coo(self, i, j, v) -> None:
         i = np.ascontiguousarray(i, np.int32)
         j = np.ascontiguousarray(j, np.int32)

@@ -10,6 +10,15 @@ to 1e-10; each step's Jacobian, right-hand side and solution become one
 training system (r1 = b - A ILU^-1 b, e1 = x* - ILU^-1 b) plus two random
 probes.  Training is Adam on the GPU with the network's own forward and
 backward kernels.
+
+With --two-level CELLS the correction is trained for the two-level cycle
+(Preconditioner 22): the Newton solves use the two-level cycle with plain
+ILU(0) (Preconditioner 21) on cells of CELLS per side, every training
+system carries those aggregates, and the loss is the energy of the error
+left after the coarse correction (gb300_mpnn_set_loss mode 1):
+
+    python -m getdp_gb300.weights.train_nl2d --n 256 --seeds 200 \
+        --two-level 8 --out getdp_gb300/weights/mpnn_nl2d_256_twolevel.npy
 """
 from __future__ import annotations
 
@@ -28,27 +37,36 @@ from .. import workloads as W
 RELAX = (1.0, 0.5, 0.25, 0.125, 0.0625, 0.03125)
 
 
-def plain_fp64():
+def plain_fp64(precond: int = 6):
     S = LA.LinAlg_CreateSolver(None)
-    for k, v in dict(Algorithm=8, Preconditioner=6, Krylov_Size=50, Nb_Iter_Max=20000,
-                     Renumbering_Technique=1, Precision=0).items():
+    for k, v in dict(Algorithm=8, Preconditioner=precond, Krylov_Size=50,
+                     Nb_Iter_Max=20000, Renumbering_Technique=1, Precision=0).items():
         S.set(k, v)
     S["stopping_test"] = 1e-10
     return S
 
 
-def dataset(n: int, seeds: int, probes: int = 2, first_seed: int = 200):
-    """(samples, number of Newton systems among them)"""
+def dataset(n: int, seeds: int, probes: int = 2, first_seed: int = 200,
+            cells: int = 0):
+    """(samples, number of Newton systems among them); cells > 0: the
+    systems carry aggregates of cells per side (two-level training)"""
     samples = []
     systems = [0]
     for s in range(seeds):
         p = W.nonlinear_2d(n=n, seed=first_seed + s)
         dm = W.dofmap_for(p)
         terms = G.DeviceTerms(p, dm)
+        agg = nc = None
+        if cells:
+            agg, nc = W.cell_aggregates(p, dm, cells)
 
         def keep(A, b, x):
-            info = LA.LinAlg_Solve(A, b, plain_fp64(), x)
+            if cells:
+                A.set_aggregates(agg, nc)
+            info = LA.LinAlg_Solve(A, b, plain_fp64(21 if cells else 6), x)
             Ac, bc, xc = LR.copy_matrix(A), LR.copy_vector(b), LR.copy_vector(x)
+            if cells:
+                Ac.set_aggregates(agg, nc)
             samples.append(LR.make_sample(Ac, bc, xc))
             systems[0] += 1
             samples.extend(LR.make_probes(Ac, probes, seed=5000 + len(samples)))
@@ -63,15 +81,20 @@ def main():
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--seeds", type=int, default=20)
     ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--two-level", type=int, default=0, metavar="CELLS",
+                    help="train for the two-level cycle on CELLS x CELLS aggregates")
     ap.add_argument("--out", required=True)
     a = ap.parse_args()
     t0 = time.time()
-    samples, systems = dataset(a.n, a.seeds)
+    samples, systems = dataset(a.n, a.seeds, cells=a.two_level)
     t1 = time.time()
     net = LR.MPNN(seed=1)
+    if a.two_level:
+        net.set_loss(1)
     hist = LR.train(net, samples, epochs=a.epochs, lr=3e-3, batch=8)
     np.save(a.out, net.params())
-    print(json.dumps({"n": a.n, "seeds": a.seeds, "systems": systems,
+    print(json.dumps({"n": a.n, "seeds": a.seeds, "two_level_cells": a.two_level,
+                      "systems": systems,
                       "samples": len(samples), "data_s": round(t1 - t0, 1),
                       "train_s": round(time.time() - t1, 1),
                       "loss": [round(h, 4) for h in hist]}))

@@ -541,6 +541,33 @@ def edge_dofmap(m: Mesh) -> DofMap:
                   edges=edges)
 
 
+def cell_aggregates(p: Problem, dm: DofMap, cells: int):
+    """Aggregates of the unknowns of a nodal scalar problem for the
+    two-level preconditioners: the cells of a uniform grid of `cells` per
+    side over the mesh's bounding box, each unknown in the cell that holds
+    its node, empty cells dropped.  Returns (agg, n_agg)."""
+    elems = p.mesh.elems
+    if dm.elem_dofs.shape[1] != elems.shape[1] or dm.ncomp != 1 or dm.nharm != 1:
+        raise ValueError("cell_aggregates: nodal scalar problems only")
+    node_of = np.full(dm.n_dof, -1, np.int64)
+    m = dm.elem_dofs >= 0
+    node_of[dm.elem_dofs[m]] = elems[m]
+    if np.any(node_of < 0):
+        raise ValueError("cell_aggregates: an unknown belongs to no element")
+    xyz = p.mesh.nodes[node_of]
+    lo = p.mesh.nodes.min(axis=0)
+    span = p.mesh.nodes.max(axis=0) - lo
+    key = np.zeros(dm.n_dof, np.int64)
+    for d in range(xyz.shape[1]):
+        if span[d] <= 0:
+            continue
+        c = np.clip(((xyz[:, d] - lo[d]) / span[d] * cells).astype(np.int64), 0, cells - 1)
+        key = key * cells + c
+    _, agg = np.unique(key, return_inverse=True)
+    agg = agg.reshape(-1).astype(np.int32)
+    return agg, int(agg.max()) + 1
+
+
 def dofmap_for(p: Problem) -> DofMap:
     g = dirichlet_coefs(p.params.get("dirichlet"))
     if p.formulation == "magnetostatics2d":

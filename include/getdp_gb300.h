@@ -339,9 +339,24 @@ int gb300_residual_noalloc(gb300_matrix *A, const gb300_vector *x,
 int gb300_matrix_set_correction(gb300_matrix *A, const double *values, int on_device);
 /* G <- s G for the attached correction (a per-system step length) */
 int gb300_matrix_scale_correction(gb300_matrix *A, double s);
+/* No counterpart in the reference (Sparskit's preconditioners are one-level).
+   Preconditioners 21 and 22 (not Sparskit values) are a two-level cycle:
+   z = S v; z += P0 Ac^-1 P0^T (v - A z); z += S (v - A z), with S = ILU(0)
+   (21) or ILU(0) followed by the learned correction (22), P0 the
+   piecewise-constant prolongation on aggregates of unknowns and
+   Ac = P0^T A P0 inverted densely on the device at every solve (with
+   Re_Use_LU, once).  gb300_matrix_set_aggregates gives the aggregate (0 ..
+   n_agg - 1) of each of A's n rows, host array; every aggregate must hold a
+   row; 1 <= n_agg <= 2048; a pattern change drops them.  A must be symmetric
+   positive definite for Ac to be (a non-positive pivot of Ac is an error). */
+int gb300_matrix_set_aggregates(gb300_matrix *A, const int *agg, int n_agg);
+/* u^T P0 Ac^-1 P0^T u for A's aggregates and its own values (the part of
+   the energy of an error e with A e = u that the coarse correction removes);
+   the coarse inverse is made at the first call and then reused. */
+int gb300_matrix_coarse_energy(gb300_matrix *A, const gb300_vector *u, double *ucu);
 /* z = M^-1 v with the preconditioner the solver would use for p
-   (Preconditioner 6 or 20; Renumbering_Technique selects the ordering) on
-   A's unscaled values. */
+   (Preconditioner 6, 20, 21 or 22; Renumbering_Technique selects the
+   ordering) on A's unscaled values. */
 int gb300_precond_apply(gb300_matrix *A, const gb300_solver_params *p,
                         const gb300_vector *v, gb300_vector *z);
 /* The network that predicts G: 3 message-passing layers of width 32 over the
@@ -367,6 +382,13 @@ int gb300_mpnn_loss_grad(gb300_mpnn *net, gb300_matrix *A, const gb300_vector *r
                          const gb300_vector *e1, int accumulate, double *loss,
                          float *grad_host);
 int gb300_mpnn_adam_step(gb300_mpnn *net, float lr, float grad_scale);
+/* The loss of gb300_mpnn_loss_grad: mode 0 (default) as above; mode 1, for
+   the correction inside the two-level cycle (Preconditioner 22), the energy
+   of the error left after the coarse correction on A's aggregates,
+   (e1 - y)^T (A - A C A) (e1 - y) / S with C = P0 Ac^-1 P0^T (the matrix
+   needs gb300_matrix_set_aggregates; its coarse inverse is made at the
+   first call and reused). */
+int gb300_mpnn_set_loss(gb300_mpnn *net, int mode);
 
 /* ---- solve ------------------------------------------------------------ */
 /* LinAlg_Solve -> solve_matrix (Sparskit.cpp:108-634) on the GPU.  A and b

@@ -2,8 +2,9 @@
 
 FP64 restatement of the learned-preconditioner network of
 getdp_gb300/csrc/learned.cu (forward pass, energy-norm loss
-(G r1 - e1)^T A (G r1 - e1) / e1^T A e1 and its gradient with respect to
-every weight, A symmetric), used to check the GPU's
+(G r1 - e1)^T A (G r1 - e1) / e1^T A e1, or its two-level form after a
+coarse correction, and its gradient with respect to every weight, A
+symmetric), used to check the GPU's
 hand-written forward and backward kernels.  Weights are used BF16-rounded
 as on the GPU unless bf16=False (for finite-difference checks of the
 gradient formulas themselves).
@@ -81,10 +82,11 @@ def forward(w, g, bf16_weights=True):
     return G, {"P": P, "h": h, "m": m}
 
 
-def loss_grad(w, g, r1, e1, A, bf16_weights=True):
+def loss_grad(w, g, r1, e1, A, bf16_weights=True, coarse=None):
     """(loss, gradient with respect to the weights, G); A is the (symmetric)
     system matrix as scipy.sparse; e1 may be None (a probe: S = r1^T D^-1
-    r1 in place of e1^T A e1)."""
+    r1 in place of e1^T A e1).  coarse = (P0, Ac^-1): the two-level loss
+    (e1 - y)^T (A - A C A) (e1 - y) / S, C = P0 Ac^-1 P0^T."""
     G, c = forward(w, g, bf16_weights)
     P, h, m = c["P"], c["h"], c["m"]
     rows, cols, e, off = g["rows"], g["cols"], g["e"], g["off"]
@@ -98,6 +100,12 @@ def loss_grad(w, g, r1, e1, A, bf16_weights=True):
     Ay = A @ y
     loss = 1.0 + (float(y @ Ay) - 2.0 * float(r1 @ y)) / S
     wv = Ay - r1
+    if coarse is not None:
+        P0, Aci = coarse
+        t = P0.T @ wv
+        ec = Aci @ t
+        loss -= float(t @ ec) / S
+        wv = wv - A @ (P0 @ ec)
     dG = 2.0 * wv[rows] * r1[cols] / S
     dg = dG * g["ds"][rows] * g["ds"][cols]
     grad = np.zeros(NPARAM)

@@ -11,6 +11,7 @@ within 1e-5 relative, gradient within 2e-3 of the largest entry.
 import numpy as np
 import pytest
 import scipy.sparse as sp
+import scipy.sparse.linalg as spla
 
 import oracle
 from getdp_gb300 import workloads as W
@@ -44,6 +45,48 @@ def test_oracle_gradient_matches_finite_differences(with_solution):
         wm[k] -= h
         fd = (M.loss_grad(wp, g, r1, e1, A, bf16_weights=False)[0] -
               M.loss_grad(wm, g, r1, e1, A, bf16_weights=False)[0]) / (2 * h)
+        assert abs(fd - grad[k]) <= 1e-6 * np.abs(grad).max() + 1e-12, (k, fd, grad[k])
+
+
+def _coarse(p, dm, ip, ix, dv, cells=3):
+    agg, nc = W.cell_aggregates(p, dm, cells)
+    A = sp.csr_matrix((dv, ix, ip))
+    P0 = sp.csr_matrix((np.ones(dm.n_dof), (np.arange(dm.n_dof), agg)),
+                       shape=(dm.n_dof, nc))
+    return agg, nc, P0, np.linalg.inv((P0.T @ A @ P0).toarray())
+
+
+@pytest.mark.parametrize("with_solution", [True, False])
+def test_oracle_two_level_gradient_matches_finite_differences(with_solution):
+    # the loss after the coarse correction, (e1 - y)^T (A - A C A) (e1 - y) / S
+    oracle.build()
+    p, dm, ip, ix, dv, _ = small_system()
+    A = sp.csr_matrix((dv, ix, ip))
+    _, _, P0, Aci = _coarse(p, dm, ip, ix, dv)
+    g = M.graph(ip, ix, dv)
+    rng = np.random.default_rng(4)
+    w = rng.standard_normal(M.NPARAM) * 0.3
+    r1 = rng.standard_normal(g["n"])
+    # the loss is written for e1 = A^-1 r1 (the error that r1 leaves)
+    e1 = spla.spsolve(A.tocsc(), r1) if with_solution else None
+    lo, grad, G = M.loss_grad(w, g, r1, e1, A, bf16_weights=False, coarse=(P0, Aci))
+    # the loss itself, written out
+    y = np.zeros(g["n"])
+    np.add.at(y, g["rows"], G * r1[g["cols"]])
+    if with_solution:
+        C = P0 @ Aci @ P0.T
+        d = e1 - y
+        want = float(d @ (A @ d) - (A @ d) @ (C @ (A @ d))) / float(e1 @ (A @ e1))
+        assert abs(lo - want) <= 1e-12 * max(1.0, abs(want))
+    idx = np.concatenate([rng.choice(M.NPARAM, 40, replace=False),
+                          [M.OFF_CO, M.OFF_BD, M.OFF_WO + 1, M.OFF_WD + 2, M.OFF_WIN]])
+    h = 1e-6
+    for k in idx:
+        wp, wm = w.copy(), w.copy()
+        wp[k] += h
+        wm[k] -= h
+        fd = (M.loss_grad(wp, g, r1, e1, A, bf16_weights=False, coarse=(P0, Aci))[0] -
+              M.loss_grad(wm, g, r1, e1, A, bf16_weights=False, coarse=(P0, Aci))[0]) / (2 * h)
         assert abs(fd - grad[k]) <= 1e-6 * np.abs(grad).max() + 1e-12, (k, fd, grad[k])
 
 
@@ -89,6 +132,38 @@ def test_gpu_forward_backward_match_oracle(with_solution):
                             sp.csr_matrix((dv, ix, ip)))
     assert abs(loss - lo) <= 1e-5 * abs(lo), (loss, lo)
     assert np.abs(grad - go).max() <= 2e-3 * np.abs(go).max(), np.abs(grad - go).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("with_solution", [True, False])
+def test_gpu_two_level_loss_matches_oracle(with_solution):
+    G, LR, LA = _gpu()
+    p, dm, ip, ix, dv, b = small_system(n=12, seed=9)
+    agg, nc, P0, Aci = _coarse(p, dm, ip, ix, dv, cells=4)
+    A = LA.gMatrix(dm.n_dof)
+    A.set_csr(ip, ix, dv)
+    A.set_aggregates(agg, nc)
+    net = LR.MPNN(seed=4)
+    net.set_loss(1)
+    rng = np.random.default_rng(6)
+    w = (rng.standard_normal(net.n_params) * 0.2).astype(np.float32)
+    net.set_params(w)
+    r1 = rng.standard_normal(dm.n_dof)
+    e1 = rng.standard_normal(dm.n_dof)
+    vr, ve = LA.gVector(dm.n_dof), LA.gVector(dm.n_dof)
+    vr.set(r1)
+    ve.set(e1)
+    loss, grad = net.loss_grad(A, vr, ve if with_solution else None, want_grad=True)
+    g = M.graph(ip, ix, dv)
+    lo, go, _ = M.loss_grad(w.astype(np.float64), g, r1, e1 if with_solution else None,
+                            sp.csr_matrix((dv, ix, ip)), coarse=(P0, Aci))
+    assert abs(loss - lo) <= 1e-5 * abs(lo), (loss, lo)
+    assert np.abs(grad - go).max() <= 2e-3 * np.abs(go).max(), np.abs(grad - go).max()
+    # the energy the coarse correction removes, u^T C u, against numpy
+    u = LA.gVector(dm.n_dof)
+    u.set(r1)
+    t = P0.T @ r1
+    assert abs(LR.coarse_energy(A, u) - t @ Aci @ t) <= 1e-9 * abs(t @ Aci @ t)
 
 
 @pytest.mark.gpu
