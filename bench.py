@@ -78,6 +78,9 @@ def parse():
     ap.add_argument("--coarse-cells", type=int, default=32,
                     help="nonlinear: cells per side of the aggregates of the two-level "
                          "preconditioner (Preconditioner 21)")
+    ap.add_argument("--learned-two-level-weights", default=None,
+                    help="nonlinear workload: also time the Newton loop with the correction "
+                         "trained for the two-level cycle (Preconditioner 22, .npy)")
     ap.add_argument("--learned-weights", default=None,
                     help="nonlinear workload: also time the Newton loop with the learned "
                          "correction (network weights, .npy)")
@@ -707,6 +710,33 @@ def run_nonlinear(args, ws, rank, local):
                        s.get("learned_attempt_iterations") or 0 for s in pol.log)),
                    "solves": pol.log, "converged": r.converged,
                    "weights": os.path.basename(args.learned_weights)}
+    learned2 = None
+    if args.learned_two_level_weights:
+        # the correction trained for the two-level cycle (Preconditioner 22),
+        # against the same cycle without it (two_level_mixed) and plain FP64
+        from getdp_gb300 import learned as LR
+        net = LR.MPNN(seed=1)
+        net.set_params(np.load(args.learned_two_level_weights))
+        p = W.nonlinear_2d(n=n, seed=5)
+        dm = W.dofmap_for(p)
+        agg, nc = W.cell_aggregates(p, dm, args.coarse_cells)
+        terms = G.DeviceTerms(p, dm)
+        runs = []
+        for _ in range(2):  # the first run also makes the network's graph buffers
+            pol = LR.TwoLevelNewtonSolver(net, agg, nc, stopping_test=1e-10, precision=1)
+            t0 = time.perf_counter()
+            r = NL.newton(terms, dm.n_dof, pol, tol_rel=1e-8, iter_max=50,
+                          relaxation=RELAX)
+            runs.append((time.perf_counter() - t0, r, pol))
+        t_l, r, pol = runs[-1]
+        learned2 = {"s": t_l, "newton_steps": len(r.history) - 1,
+                    "linear_iterations": int(sum(s["iterations"] for s in r.solves)),
+                    "learned_attempt_iterations": int(sum(
+                        s.get("learned_attempt_iterations") or 0 for s in pol.log)),
+                    "solves": pol.log, "converged": r.converged, "aggregates": nc,
+                    "speedup_vs_plain_fp64": res[0]["s"] / t_l,
+                    "speedup_vs_two_level_mixed": two[1]["s"] / t_l,
+                    "weights": os.path.basename(args.learned_two_level_weights)}
     line = {"metric": "nonlinear 2D magnetostatics: time to 1e-8 Newton residual "
                       "(Generate + Solve per step)",
             "value": best["s"], "unit": "s", "n_gpus": ws, "steps": args.steps,
@@ -726,6 +756,8 @@ def run_nonlinear(args, ws, rank, local):
             "mixed_coloured_scatter": deterministic}
     if learned is not None:
         line["learned_mixed"] = learned
+    if learned2 is not None:
+        line["learned_two_level_mixed"] = learned2
     if not args.skip_cpu and rank == 0:
         import oracle
         oracle.build()

@@ -463,7 +463,8 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
     }
   }
   int zr = 0;
-  GB_TRY(ilu_factor(M, M->val.p, fp32, &zr));
+  // Re_Use_LU: keep the factor of the previous call (same pattern)
+  GB_TRY(ilu_factor(M, M->val.p, fp32, &zr, p->re_use_lu != 0));
   if(zr) {
     set_error("Zero pivot on line %d in ILU", zr);
     return GB300_ERR_ZERO_PIVOT;
@@ -473,7 +474,7 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
     if(learned) correction_apply(M, M->val.p, vv, zz, t1.p, t2.p, nullptr, st);
   };
   if(coarse) {
-    GB_TRY(coarse_setup(M, M->val.p, false));
+    GB_TRY(coarse_setup(M, M->val.p, p->re_use_lu != 0));
     two_level_apply(M, M->val.p, vin, zout, t3.p, t4.p, nullptr, st, smooth);
   }
   else

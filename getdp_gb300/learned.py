@@ -186,7 +186,7 @@ def coarse_energy(A: LA.gMatrix, u: LA.gVector) -> float:
     return out.value
 
 
-def step_length_two_level(A: LA.gMatrix, probes: int = 2, seed: int = 0,
+def step_length_two_level(A: LA.gMatrix, probes: int = 1, seed: int = 0,
                           renumbering: int = 1, precision: int = 0) -> float:
     """step_length for the correction inside the two-level cycle: the step
     w that minimises the energy of the error left after the coarse
@@ -202,10 +202,12 @@ def step_length_two_level(A: LA.gMatrix, probes: int = 2, seed: int = 0,
     S20 = ilu_params(renumbering)
     S20.set("Preconditioner", 20)
     S20.set("Precision", precision)
+    S20["re_use_lu"] = 1  # the factor the first application made
     v, z1, z2, r1, ag, sm = (LA.gVector(n) for _ in range(6))
     num = den = 0.0
-    for _ in range(probes):
+    for k in range(probes):
         v.set(rng.standard_normal(n))
+        S6["re_use_lu"] = 1 if k else 0  # factor A's current values once
         check(L.gb300_precond_apply(A.h, ctypes.byref(S6.params), v.h, z1.h))
         check(L.gb300_precond_apply(A.h, ctypes.byref(S20.params), v.h, z2.h))
         check(L.gb300_vector_axpby(-1.0, z1.h, 1.0, z2.h))    # g = z2 - z1

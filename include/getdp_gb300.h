@@ -356,7 +356,8 @@ int gb300_matrix_set_aggregates(gb300_matrix *A, const int *agg, int n_agg);
 int gb300_matrix_coarse_energy(gb300_matrix *A, const gb300_vector *u, double *ucu);
 /* z = M^-1 v with the preconditioner the solver would use for p
    (Preconditioner 6, 20, 21 or 22; Renumbering_Technique selects the
-   ordering) on A's unscaled values. */
+   ordering) on A's unscaled values; with p->re_use_lu the factor (and
+   coarse inverse) of the previous call on A's pattern is kept. */
 int gb300_precond_apply(gb300_matrix *A, const gb300_solver_params *p,
                         const gb300_vector *v, gb300_vector *z);
 /* The network that predicts G: 3 message-passing layers of width 32 over the
