@@ -417,6 +417,29 @@ def run_other(args, ws, rank, local):
                      "solve_s": ts / args.steps, "iterations": inf["iterations"],
                      "status": inf["status"],
                      "true_rel_residual": inf["true_residual"] / max(inf["rhs_norm"], 1e-300)}
+    two = None
+    if args.workload == "magnetostatics2d":
+        # the two-level cycle (Preconditioner 21) on aggregates of 8 x 8 nodes
+        agg, nc = W.cell_aggregates(p, dm, max(1, min(n // 8, 45)))
+        S = params(0)
+        S.set("Preconditioner", 21)
+        for _ in range(args.warmup):
+            G.generate(A, b, terms.batch, pattern=True)
+            A.set_aggregates(agg, nc)
+            LA.LinAlg_Solve(A, b, S, x)
+        tg = ts = 0.0
+        for _ in range(args.steps):
+            ev(0)
+            G.generate(A, b, terms.batch, pattern=True)
+            ev(1)
+            A.set_aggregates(agg, nc)
+            inf = LA.LinAlg_Solve(A, b, S, x)
+            ev(2)
+            tg += elapsed(0, 1)
+            ts += elapsed(1, 2)
+        two = {"s": (tg + ts) / args.steps, "solve_s": ts / args.steps,
+               "iterations": inf["iterations"], "status": inf["status"], "aggregates": nc,
+               "true_rel_residual": inf["true_residual"] / max(inf["rhs_norm"], 1e-300)}
     best = res[precisions[-1]]
     line = {"metric": metric, "value": best["s"], "unit": "s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": best["s"] * 1e3,
@@ -426,6 +449,8 @@ def run_other(args, ws, rank, local):
             "config": {"workload": desc, "elements": p.mesh.n_elems, "unknowns": N,
                        "nnz": A.nnz(), "parallelism": f"replicas x{ws}"},
             "fp64": res[0], "mixed": res.get(1)}
+    if two is not None:
+        line["two_level_fp64"] = two
     if not args.skip_cpu and rank == 0:
         import oracle
         oracle.build()

@@ -113,6 +113,7 @@ int coarse_set(gb300_matrix *A, const int *agg, int nc)
   GB_TRY(c->ec.alloc(nc));
   GB_TRY(c->err.alloc(1));
   GB_TRY(c->amax.alloc(1));
+  GB_TRY(c->part.alloc(kReduceBlocks));
   GB_CUDA(cudaMemcpyAsync(c->agg.p, agg, sizeof(int) * n, cudaMemcpyHostToDevice, st));
   GB_CUDA(cudaMemcpyAsync(c->aperm.p, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice,
                           st));
@@ -160,6 +161,7 @@ int coarse_follow(const gb300_matrix *A, gb300_matrix *B, const Colouring *C,
   GB_TRY(c->ec.alloc(nc));
   GB_TRY(c->err.alloc(1));
   GB_TRY(c->amax.alloc(1));
+  GB_TRY(c->part.alloc(kReduceBlocks));
   k_follow_agg<<<grid_for(n, 256), 256, 0, st>>>(n, C->old_of.p, a->agg.p, C->new_of.p,
                                                  a->aperm.p, c->agg.p, c->aperm.p);
   GB_CUDA(cudaMemcpyAsync(c->aptr.p, a->aptr.p, sizeof(int) * (nc + 1),
@@ -316,14 +318,6 @@ int coarse_setup(gb300_matrix *A, const double *val, bool reuse)
 // ---------------------------------------------------------------------------
 // application
 
-__global__ void k_resid_into(int n, const double *__restrict__ v, double *__restrict__ t,
-                             const int *flag)
-{
-  if(flag && !*flag) return;
-  for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    t[i] = v[i] - t[i];
-}
-
 __global__ void k_add_into(int n, const double *__restrict__ t, double *__restrict__ z,
                            const int *flag)
 {
@@ -380,8 +374,7 @@ void coarse_correct(const gb300_matrix *A, const double *val, const double *v, d
   const Coarse *c = A->coarse;
   const int n = A->n, nc = c->nc;
   const int g = grid_for(n, 256, kReduceBlocks * 4);
-  spmv_guarded(A, val, z, t, flag, st);
-  k_resid_into<<<g, 256, 0, st>>>(n, v, t, flag);
+  residual64_guarded(A, val, z, v, t, c->part.p, flag, st);  // t = v - A z
   k_restrict<<<grid_for((long long)nc * 32, 256), 256, 0, st>>>(nc, c->aptr.p, c->aperm.p,
                                                                 t, c->rc.p, flag);
   k_coarse_gemv<<<grid_for((long long)nc * 32, 256), 256, 0, st>>>(nc, c->inv.p, c->rc.p,
@@ -460,8 +453,7 @@ void two_level_apply(const gb300_matrix *A, const double *val, const double *v, 
   const int g = grid_for(n, 256, kReduceBlocks * 4);
   smooth(v, z);
   coarse_correct(A, val, v, z, t3, flag, st);
-  spmv_guarded(A, val, z, t3, flag, st);
-  k_resid_into<<<g, 256, 0, st>>>(n, v, t3, flag);
+  residual64_guarded(A, val, z, v, t3, A->coarse->part.p, flag, st);  // t3 = v - A z
   smooth(t3, t4);
   k_add_into<<<g, 256, 0, st>>>(n, t4, z, flag);
 }

@@ -84,6 +84,7 @@ struct Coarse {
   DevBuf<double> rc, ec;          // coarse residual and correction
   DevBuf<int> err;
   DevBuf<double> amax;
+  DevBuf<double> part;            // partial sums of the fused residual products
 };
 void coarse_free(Coarse *c);
 bool coarse_valid(const gb300_matrix *A);
