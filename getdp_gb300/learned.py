@@ -131,6 +131,23 @@ def make_probes(A: LA.gMatrix, count: int, seed: int, renumbering: int = 1) -> l
     return out
 
 
+def make_error_probes(A: LA.gMatrix, count: int, seed: int, renumbering: int = 1) -> list:
+    """Random probes with a known solution: e0 random, b = A e0, then as
+    make_sample (z1 = ILU^-1 b, r1 = b - A z1 = A e1, e1 = e0 - z1), so
+    that r1 = A e1 holds exactly, as the two-level loss needs."""
+    L = _lib.load()
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        e0 = LA.gVector(A.n)
+        e0.set(rng.standard_normal(A.n))
+        e0._flush()
+        b = LA.gVector(A.n)
+        check(L.gb300_matrix_mult(A.h, e0.h, b.h))
+        out.append(make_sample(A, b, e0, renumbering))
+    return out
+
+
 def copy_matrix(A: LA.gMatrix) -> LA.gMatrix:
     """A new matrix with A's CSR (through the host): training keeps the
     Jacobians of every Newton step while the solver reuses A."""
@@ -332,13 +349,14 @@ class TwoLevelNewtonSolver:
     for nonlinear.newton.  The method without the network is the same cycle
     with plain ILU(0) smoothing (Preconditioner 21): it is used when the
     energy-optimal step of the correction is below min_step, when the
-    learned solve does not converge within the last plain step count (the
-    first time, first_cap), and for good after max_failures such attempts.
+    learned solve does not converge within the last plain step count, and
+    for good after max_failures such attempts; the first solve runs it to
+    set that count.
     The FP64 residual decides in every case."""
 
     def __init__(self, net: MPNN, agg, n_agg: int, stopping_test: float = 1e-10,
                  krylov: int = 50, nb_iter_max: int = 20000, precision: int = 1,
-                 first_cap: int = 2000, max_failures: int = 1, min_step: float = 0.05):
+                 max_failures: int = 1, min_step: float = 0.05):
         self.net = net
         self.agg = np.ascontiguousarray(agg, np.int32)
         self.n_agg = int(n_agg)
@@ -346,7 +364,6 @@ class TwoLevelNewtonSolver:
         self.krylov = krylov
         self.nb_iter_max = nb_iter_max
         self.precision = precision
-        self.first_cap = first_cap
         self.max_failures = max_failures
         self.min_step = min_step
         self.failures = 0
@@ -374,7 +391,10 @@ class TwoLevelNewtonSolver:
         if self.seen is not A:
             A.set_aggregates(self.agg, self.n_agg)
             self.seen = A
-        if self.failures >= self.max_failures:
+        if self.last_plain is None:
+            # the first solve sets the step count the learned attempts must beat
+            info = self._plain(A, b, x, "two-level ilu0 (reference count)", {})
+        elif self.failures >= self.max_failures:
             info = self._plain(A, b, x, "two-level ilu0 (learned off)", {})
         else:
             self.net.infer(A)
@@ -385,8 +405,7 @@ class TwoLevelNewtonSolver:
                 self.failures += 1
             else:
                 check(_lib.load().gb300_matrix_scale_correction(A.h, ctypes.c_double(omega)))
-                cap = self.last_plain if self.last_plain else self.first_cap
-                info = LA.LinAlg_Solve(A, b, self._params(22, cap), x)
+                info = LA.LinAlg_Solve(A, b, self._params(22, self.last_plain), x)
                 info["preconditioner"] = "two-level learned"
                 info["step"] = omega
                 if info["status"] != 0:

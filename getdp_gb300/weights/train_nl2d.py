@@ -14,8 +14,9 @@ backward kernels.
 With --two-level CELLS the correction is trained for the two-level cycle
 (Preconditioner 22): the Newton solves use the two-level cycle with plain
 ILU(0) (Preconditioner 21) on cells of CELLS per side, every training
-system carries those aggregates, and the loss is the energy of the error
-left after the coarse correction (gb300_mpnn_set_loss mode 1):
+system carries those aggregates, the probes are random errors e0 with
+b = A e0 (so that r1 = A e1 exactly), and the loss is the energy of the
+error left after the coarse correction (gb300_mpnn_set_loss mode 1):
 
     python -m getdp_gb300.weights.train_nl2d --n 256 --seeds 200 \
         --two-level 8 --out getdp_gb300/weights/mpnn_nl2d_256_twolevel.npy
@@ -69,7 +70,10 @@ def dataset(n: int, seeds: int, probes: int = 2, first_seed: int = 200,
                 Ac.set_aggregates(agg, nc)
             samples.append(LR.make_sample(Ac, bc, xc))
             systems[0] += 1
-            samples.extend(LR.make_probes(Ac, probes, seed=5000 + len(samples)))
+            if cells:  # the two-level loss needs r1 = A e1 exactly
+                samples.extend(LR.make_error_probes(Ac, probes, seed=5000 + len(samples)))
+            else:
+                samples.extend(LR.make_probes(Ac, probes, seed=5000 + len(samples)))
             return info
 
         NL.newton(terms, dm.n_dof, keep, tol_rel=1e-8, iter_max=50, relaxation=RELAX)

@@ -182,3 +182,19 @@ def test_indefinite_coarse_matrix_is_an_error():
     x = LA.gVector(m * m)
     with pytest.raises(LA.GetDPError, match="not positive definite"):
         LA.LinAlg_Solve(A, b, _params(21, 0), x)
+
+
+def test_zero_correction_gives_the_plain_cycle():
+    # Preconditioner 22 with G = 0 is Preconditioner 21, step for step
+    p, dm, A, b, _ = _system(64, state_scale=0.02)
+    agg, nc = W.cell_aggregates(p, dm, 8)
+    A.set_aggregates(agg, nc)
+    nnz = A.nnz()
+    _lib.check(_lib.load().gb300_matrix_set_correction(
+        A.h, np.zeros(nnz).ctypes.data_as(ctypes.c_void_p), 0))
+    for prec in (0, 1):
+        x21, i21 = _solve(A, b, _params(21, 1, 9, prec))
+        x22, i22 = _solve(A, b, _params(22, 1, 9, prec))
+        assert i21["status"] == 0 and i22["status"] == 0
+        assert i21["iterations"] == i22["iterations"]
+        assert np.array_equal(x21, x22)
