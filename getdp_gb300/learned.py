@@ -204,13 +204,19 @@ def coarse_energy(A: LA.gMatrix, u: LA.gVector) -> float:
 
 
 def step_length_two_level(A: LA.gMatrix, probes: int = 1, seed: int = 0,
-                          renumbering: int = 1, precision: int = 0) -> float:
+                          renumbering: int = 1, precision: int = 0,
+                          rhs: LA.gVector = None) -> float:
     """step_length for the correction inside the two-level cycle: the step
     w that minimises the energy of the error left after the coarse
-    correction, (e1 - w g)^T (A - A C A) (e1 - w g), over random probes:
+    correction, (e1 - w g)^T (A - A C A) (e1 - w g), over the probes:
     w = (g.r1 - (Ag)^T C r1) / (g.Ag - (Ag)^T C Ag), the cross term by
-    polarisation, 2 u^T C v = (u+v)^T C (u+v) - u^T C u - v^T C v.  A needs
-    aggregates and the correction."""
+    polarisation, 2 u^T C v = (u+v)^T C (u+v) - u^T C u - v^T C v (no
+    solution needed: e1^T A g = r1^T g).  With rhs, the probe is the
+    system's own right-hand side, whose error after the ILU(0) step is the
+    one the solve meets (random probes are white noise, which a local
+    correction removes far better: they overstate the step about twofold);
+    otherwise `probes` random vectors.  A needs aggregates and the
+    correction."""
     L = _lib.load()
     rng = np.random.default_rng(seed)
     n = A.n
@@ -222,8 +228,12 @@ def step_length_two_level(A: LA.gMatrix, probes: int = 1, seed: int = 0,
     S20["re_use_lu"] = 1  # the factor the first application made
     v, z1, z2, r1, ag, sm = (LA.gVector(n) for _ in range(6))
     num = den = 0.0
-    for k in range(probes):
-        v.set(rng.standard_normal(n))
+    for k in range(1 if rhs is not None else probes):
+        if rhs is not None:
+            rhs._flush()
+            check(L.gb300_vector_axpby(1.0, rhs.h, 0.0, v.h))
+        else:
+            v.set(rng.standard_normal(n))
         S6["re_use_lu"] = 1 if k else 0  # factor A's current values once
         check(L.gb300_precond_apply(A.h, ctypes.byref(S6.params), v.h, z1.h))
         check(L.gb300_precond_apply(A.h, ctypes.byref(S20.params), v.h, z2.h))
@@ -398,7 +408,7 @@ class TwoLevelNewtonSolver:
             info = self._plain(A, b, x, "two-level ilu0 (learned off)", {})
         else:
             self.net.infer(A)
-            omega = step_length_two_level(A, precision=self.precision)
+            omega = step_length_two_level(A, precision=self.precision, rhs=b)
             if omega < self.min_step:
                 info = self._plain(A, b, x, "two-level ilu0 (correction rejected)",
                                    dict(step=omega, learned_attempt_iterations=0))
