@@ -113,7 +113,6 @@ int coarse_set(gb300_matrix *A, const int *agg, int nc)
   GB_TRY(c->ec.alloc(nc));
   GB_TRY(c->err.alloc(1));
   GB_TRY(c->amax.alloc(1));
-  GB_TRY(c->part.alloc(kReduceBlocks));
   GB_CUDA(cudaMemcpyAsync(c->agg.p, agg, sizeof(int) * n, cudaMemcpyHostToDevice, st));
   GB_CUDA(cudaMemcpyAsync(c->aperm.p, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice,
                           st));
@@ -161,7 +160,6 @@ int coarse_follow(const gb300_matrix *A, gb300_matrix *B, const Colouring *C,
   GB_TRY(c->ec.alloc(nc));
   GB_TRY(c->err.alloc(1));
   GB_TRY(c->amax.alloc(1));
-  GB_TRY(c->part.alloc(kReduceBlocks));
   k_follow_agg<<<grid_for(n, 256), 256, 0, st>>>(n, C->old_of.p, a->agg.p, C->new_of.p,
                                                  a->aperm.p, c->agg.p, c->aperm.p);
   GB_CUDA(cudaMemcpyAsync(c->aptr.p, a->aptr.p, sizeof(int) * (nc + 1),
@@ -374,7 +372,7 @@ void coarse_correct(const gb300_matrix *A, const double *val, const double *v, d
   const Coarse *c = A->coarse;
   const int n = A->n, nc = c->nc;
   const int g = grid_for(n, 256, kReduceBlocks * 4);
-  residual64_guarded(A, val, z, v, t, c->part.p, flag, st);  // t = v - A z
+  resid_guarded(A, val, z, v, t, flag, st);  // t = v - A z
   k_restrict<<<grid_for((long long)nc * 32, 256), 256, 0, st>>>(nc, c->aptr.p, c->aperm.p,
                                                                 t, c->rc.p, flag);
   k_coarse_gemv<<<grid_for((long long)nc * 32, 256), 256, 0, st>>>(nc, c->inv.p, c->rc.p,
@@ -447,14 +445,15 @@ int coarse_energy(gb300_matrix *A, const double *u, double *ucu_dev, cudaStream_
 
 void two_level_apply(const gb300_matrix *A, const double *val, const double *v, double *z,
                      double *t3, double *t4, const int *flag, cudaStream_t st,
-                     const std::function<void(const double *, double *)> &smooth)
+                     const std::function<void(const double *, double *)> &smooth,
+                     const std::function<void(const double *, double *)> &smooth_post)
 {
   const int n = A->n;
   const int g = grid_for(n, 256, kReduceBlocks * 4);
   smooth(v, z);
   coarse_correct(A, val, v, z, t3, flag, st);
-  residual64_guarded(A, val, z, v, t3, A->coarse->part.p, flag, st);  // t3 = v - A z
-  smooth(t3, t4);
+  resid_guarded(A, val, z, v, t3, flag, st);  // t3 = v - A z
+  smooth_post(t3, t4);
   k_add_into<<<g, 256, 0, st>>>(n, t4, z, flag);
 }
 

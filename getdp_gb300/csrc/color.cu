@@ -412,9 +412,12 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
   cudaStream_t st = A->ctx->stream;
   const int n = A->n;
   const bool learned = (p->preconditioner == kPrecondLearned ||
-                        p->preconditioner == kPrecondLearnedCoarse);
+                        p->preconditioner == kPrecondLearnedCoarse ||
+                        p->preconditioner == kPrecondLearnedCoarsePre);
   const bool coarse = (p->preconditioner == kPrecondCoarse ||
-                       p->preconditioner == kPrecondLearnedCoarse);
+                       p->preconditioner == kPrecondLearnedCoarse ||
+                       p->preconditioner == kPrecondLearnedCoarsePre);
+  const bool learned_post = learned && p->preconditioner != kPrecondLearnedCoarsePre;
   if(p->preconditioner != 6 && !learned && !coarse) {
     set_error("preconditioner apply: Preconditioner %d is not an ILU(0)", p->preconditioner);
     return GB300_ERR_UNSUPPORTED;
@@ -469,16 +472,18 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
     set_error("Zero pivot on line %d in ILU", zr);
     return GB300_ERR_ZERO_PIVOT;
   }
-  auto smooth = [&](const double *vv, double *zz) {
+  auto smooth = [&](const double *vv, double *zz, bool corr) {
     ilu_apply(M, fp32, vv, zz, fp32 ? t32.p : nullptr, nullptr, st);
-    if(learned) correction_apply(M, M->val.p, vv, zz, t1.p, t2.p, nullptr, st);
+    if(corr) correction_apply(M, M->val.p, vv, zz, t1.p, t2.p, nullptr, st);
   };
   if(coarse) {
     GB_TRY(coarse_setup(M, M->val.p, p->re_use_lu != 0));
-    two_level_apply(M, M->val.p, vin, zout, t3.p, t4.p, nullptr, st, smooth);
+    two_level_apply(M, M->val.p, vin, zout, t3.p, t4.p, nullptr, st,
+                    [&](const double *vv, double *zz) { smooth(vv, zz, learned); },
+                    [&](const double *vv, double *zz) { smooth(vv, zz, learned_post); });
   }
   else
-    smooth(vin, zout);
+    smooth(vin, zout, learned);
   if(C) unpermute_solution(C, zout, z, st);
   GB_CUDA(cudaGetLastError());
   GB_CUDA(cudaStreamSynchronize(st));

@@ -934,35 +934,14 @@ bool correction_valid(const gb300_matrix *A)
   return A->corr_version == A->pattern_version && A->corr.p && A->nnz > 0;
 }
 
-// r1 = v - A z
-__global__ void k_sub_from(int n, const double *__restrict__ v, double *__restrict__ t,
-                           const int *flag)
-{
-  if(flag && !*flag) return;
-  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-      i += (long long)gridDim.x * blockDim.x)
-    t[i] = v[i] - t[i];
-}
-
-__global__ void k_add_to(int n, const double *__restrict__ t, double *__restrict__ z,
-                         const int *flag)
-{
-  if(flag && !*flag) return;
-  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-      i += (long long)gridDim.x * blockDim.x)
-    z[i] += t[i];
-}
-
-// z <- z + G (v - A z): the learned correction after the ILU(0) step
+// z <- z + G (v - A z): the learned correction after the ILU(0) step (two
+// fused products: t1 = v - A z, then z += G t1; t2 is not needed)
 void correction_apply(const gb300_matrix *A, const double *val, const double *v,
                       double *z, double *t1, double *t2, const int *flag, cudaStream_t st)
 {
-  const int n = A->n;
-  const int g = grid_for(n, 256, kReduceBlocks * 4);
-  spmv_guarded(A, val, z, t1, flag, st);
-  k_sub_from<<<g, 256, 0, st>>>(n, v, t1, flag);
-  spmv_guarded(A, A->corr.p, t1, t2, flag, st);
-  k_add_to<<<g, 256, 0, st>>>(n, t2, z, flag);
+  (void)t2;
+  resid_guarded(A, val, z, v, t1, flag, st);
+  spmv_add_guarded(A, A->corr.p, t1, z, flag, st);
 }
 
 int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
@@ -985,9 +964,12 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   // 20: ILU(0) followed by the learned correction on A's pattern; 21, 22:
   // the two-level cycle on aggregates around ILU(0) (22: and the correction)
   const bool learned = (p->preconditioner == kPrecondLearned ||
-                        p->preconditioner == kPrecondLearnedCoarse);
+                        p->preconditioner == kPrecondLearnedCoarse ||
+                        p->preconditioner == kPrecondLearnedCoarsePre);
   const bool coarse = (p->preconditioner == kPrecondCoarse ||
-                       p->preconditioner == kPrecondLearnedCoarse);
+                       p->preconditioner == kPrecondLearnedCoarse ||
+                       p->preconditioner == kPrecondLearnedCoarsePre);
+  const bool learned_post = learned && p->preconditioner != kPrecondLearnedCoarsePre;
   bool precond = (p->preconditioner == 6) || learned || coarse;
   if(p->preconditioner != 0 && p->preconditioner != 6 && p->preconditioner != 8 &&
      !learned && !coarse) {
@@ -1049,20 +1031,21 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   // one per 2048 rows up to kReduceBlocks (small systems keep the
   // one-block reductions short); fixed for a given n, so deterministic
   const int nb = std::min(kReduceBlocks, std::max(152, (n + 2047) / 2048));
-  auto smooth = [&](const double *v, double *z, const int *flag) {
+  auto smooth = [&](const double *v, double *z, const int *flag, bool corr) {
     if(precond)
       ilu_apply(A, fp32, v, z, t32, flag, st);
     else
       k_cvt<double, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, z, flag);
-    if(learned) correction_apply(A, val, v, z, t1, t2, flag, st);
+    if(corr) correction_apply(A, val, v, z, t1, t2, flag, st);
   };
   auto precond_apply = [&](const double *v, double *z, const int *flag) {
     if(!coarse) {
-      smooth(v, z, flag);
+      smooth(v, z, flag, learned);
       return;
     }
     two_level_apply(A, val, v, z, t3, t4, flag, st,
-                    [&](const double *vv, double *zz) { smooth(vv, zz, flag); });
+                    [&](const double *vv, double *zz) { smooth(vv, zz, flag, learned); },
+                    [&](const double *vv, double *zz) { smooth(vv, zz, flag, learned_post); });
   };
 
   cudaGraph_t graph;

@@ -902,7 +902,8 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
     bool used = false;
     if(p->renumbering_technique == 1 &&
        (p->preconditioner == 6 || p->preconditioner == kPrecondLearned ||
-        p->preconditioner == kPrecondCoarse || p->preconditioner == kPrecondLearnedCoarse)) {
+        p->preconditioner == kPrecondCoarse || p->preconditioner == kPrecondLearnedCoarse ||
+        p->preconditioner == kPrecondLearnedCoarsePre)) {
       rc = gmres_solve_coloured(A, val, rhs, x, p, info, W, &used);
       if(rc != GB300_OK) return rc;
     }

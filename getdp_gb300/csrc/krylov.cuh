@@ -70,6 +70,9 @@ constexpr int kPrecondLearned = 20;
 // the learned correction (22) (coarse.cu)
 constexpr int kPrecondCoarse = 21;
 constexpr int kPrecondLearnedCoarse = 22;
+// 23: as 22 with the correction in the first smoothing only (the half of
+// the cycle its loss is trained on; half its cost)
+constexpr int kPrecondLearnedCoarsePre = 23;
 constexpr int kMaxCoarse = 2048;  // dense coarse inverse: at most 32 MiB
 struct Coarse {
   int n = 0, nc = 0;
@@ -84,7 +87,6 @@ struct Coarse {
   DevBuf<double> rc, ec;          // coarse residual and correction
   DevBuf<int> err;
   DevBuf<double> amax;
-  DevBuf<double> part;            // partial sums of the fused residual products
 };
 void coarse_free(Coarse *c);
 bool coarse_valid(const gb300_matrix *A);
@@ -101,9 +103,11 @@ int coarse_energy_project(gb300_matrix *A, double *w, double *t, double *q, doub
                           cudaStream_t st);
 // *ucu_dev = u^T C u (same coarse inverse as coarse_energy_project)
 int coarse_energy(gb300_matrix *A, const double *u, double *ucu_dev, cudaStream_t st);
+// smooth: the first smoothing, smooth_post: the second
 void two_level_apply(const gb300_matrix *A, const double *val, const double *v, double *z,
                      double *t3, double *t4, const int *flag, cudaStream_t st,
-                     const std::function<void(const double *, double *)> &smooth);
+                     const std::function<void(const double *, double *)> &smooth,
+                     const std::function<void(const double *, double *)> &smooth_post);
 bool correction_valid(const gb300_matrix *A);
 void correction_apply(const gb300_matrix *A, const double *val, const double *v,
                       double *z, double *t1, double *t2, const int *flag, cudaStream_t st);

@@ -513,13 +513,17 @@ k_spmv(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
         y[row] = r;
         red += r * r;
       }
+      else if(MODE == 3)  // y += A x
+        y[row] += sum;
+      else if(MODE == 4)  // y = b - A x, no partial sums
+        y[row] = b[row] - sum;
       else {
         y[row] = sum;
         if(MODE == 2) red += x[row] * sum;
       }
     }
   }
-  if(MODE != 0) {
+  if(MODE == 1 || MODE == 2) {
     double s = block_sum<double, 256>((double)red);
     if(threadIdx.x == 0) part[blockIdx.x] = s;
   }
@@ -532,9 +536,10 @@ static void launch_spmv(const gb300_matrix *A, const V *val, const XT *x,
 {
   int n = A->n;
   int rows_per_block_64 = 256 / A->tpr;
-  int blocks = (MODE == 0) ? grid_for(n, rows_per_block_64, 1 << 30)
-                           : kReduceBlocks;
-  if(MODE == 0 && blocks > 152 * 64) blocks = 152 * 64;
+  // modes with partial sums (1, 2) run on the fixed reduction grid
+  constexpr bool kFree = (MODE == 0 || MODE == 3 || MODE == 4);
+  int blocks = kFree ? grid_for(n, rows_per_block_64, 1 << 30) : kReduceBlocks;
+  if(kFree && blocks > 152 * 64) blocks = 152 * 64;
   switch(A->tpr) {
   case 2:
     k_spmv<2, MODE><<<blocks, 256, 0, st>>>(n, A->rowptr.p, A->col.p, val, x, b, y, part, flag);
@@ -588,6 +593,16 @@ void spmv_guarded(const gb300_matrix *A, const double *val, const double *x,
                   double *y, const int *flag, cudaStream_t st)
 {
   launch_spmv<0, double, double>(A, val, x, nullptr, y, nullptr, st, flag);
+}
+void spmv_add_guarded(const gb300_matrix *A, const double *val, const double *x,
+                      double *y, const int *flag, cudaStream_t st)
+{
+  launch_spmv<3, double, double>(A, val, x, nullptr, y, nullptr, st, flag);
+}
+void resid_guarded(const gb300_matrix *A, const double *val, const double *x,
+                   const double *b, double *r, const int *flag, cudaStream_t st)
+{
+  launch_spmv<4, double, double>(A, val, x, b, r, nullptr, st, flag);
 }
 
 // sum of the fixed-size partial array, in a fixed order, into *out

@@ -21,6 +21,11 @@ void spmv_plain(const gb300_matrix *A, const double *val, const double *x,
                 double *y, cudaStream_t st);
 void spmv_guarded(const gb300_matrix *A, const double *val, const double *x,
                   double *y, const int *flag, cudaStream_t st);
+// y += A x, and r = b - A x without partial sums (guarded by *flag)
+void spmv_add_guarded(const gb300_matrix *A, const double *val, const double *x,
+                      double *y, const int *flag, cudaStream_t st);
+void resid_guarded(const gb300_matrix *A, const double *val, const double *x,
+                   const double *b, double *r, const int *flag, cudaStream_t st);
 void residual64(const gb300_matrix *A, const double *val, const double *x,
                 const double *b, double *r, double *part, cudaStream_t st);
 void residual64_guarded(const gb300_matrix *A, const double *val,

@@ -356,17 +356,21 @@ class NewtonSolver:
 class TwoLevelNewtonSolver:
     """The linear solve of each Newton step with the learned correction
     inside the two-level cycle (Preconditioner 22, FGMRES), as a callable
-    for nonlinear.newton.  The method without the network is the same cycle
-    with plain ILU(0) smoothing (Preconditioner 21): it is used when the
-    energy-optimal step of the correction is below min_step, when the
-    learned solve does not converge within the last plain step count, and
-    for good after max_failures such attempts; the first solve runs it to
-    set that count.
-    The FP64 residual decides in every case."""
+    for nonlinear.newton.  The correction is used at the scale it was
+    trained for (step 1: the training loss is the energy the cycle leaves);
+    step=None scales it by step_length_two_level on the right-hand side,
+    which measured 7-9 on the nonlinear Jacobians and made FGMRES fail.
+    The method without the network is the same cycle with plain ILU(0)
+    smoothing (Preconditioner 21): it is used when the step is below
+    min_step, when the learned solve does not converge within the last
+    plain step count, and for good after max_failures such attempts; the
+    first solve runs it to set that count.  The FP64 residual decides in
+    every case."""
 
     def __init__(self, net: MPNN, agg, n_agg: int, stopping_test: float = 1e-10,
                  krylov: int = 50, nb_iter_max: int = 20000, precision: int = 1,
-                 max_failures: int = 1, min_step: float = 0.05):
+                 max_failures: int = 1, min_step: float = 0.05, step: float = 1.0,
+                 preconditioner: int = 22):
         self.net = net
         self.agg = np.ascontiguousarray(agg, np.int32)
         self.n_agg = int(n_agg)
@@ -376,6 +380,8 @@ class TwoLevelNewtonSolver:
         self.precision = precision
         self.max_failures = max_failures
         self.min_step = min_step
+        self.step = step
+        self.preconditioner = preconditioner  # 22, or 23: first smoothing only
         self.failures = 0
         self.last_plain = None
         self.seen = None
@@ -408,14 +414,19 @@ class TwoLevelNewtonSolver:
             info = self._plain(A, b, x, "two-level ilu0 (learned off)", {})
         else:
             self.net.infer(A)
-            omega = step_length_two_level(A, precision=self.precision, rhs=b)
+            omega = self.step
+            if omega is None:
+                omega = step_length_two_level(A, precision=self.precision, rhs=b)
             if omega < self.min_step:
                 info = self._plain(A, b, x, "two-level ilu0 (correction rejected)",
                                    dict(step=omega, learned_attempt_iterations=0))
                 self.failures += 1
             else:
-                check(_lib.load().gb300_matrix_scale_correction(A.h, ctypes.c_double(omega)))
-                info = LA.LinAlg_Solve(A, b, self._params(22, self.last_plain), x)
+                if omega != 1.0:
+                    check(_lib.load().gb300_matrix_scale_correction(A.h,
+                                                                    ctypes.c_double(omega)))
+                info = LA.LinAlg_Solve(A, b, self._params(self.preconditioner, self.last_plain),
+                                       x)
                 info["preconditioner"] = "two-level learned"
                 info["step"] = omega
                 if info["status"] != 0:

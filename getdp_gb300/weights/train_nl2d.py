@@ -85,12 +85,14 @@ def main():
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--seeds", type=int, default=20)
     ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--probes", type=int, default=2,
+                    help="random probes per Newton system")
     ap.add_argument("--two-level", type=int, default=0, metavar="CELLS",
                     help="train for the two-level cycle on CELLS x CELLS aggregates")
     ap.add_argument("--out", required=True)
     a = ap.parse_args()
     t0 = time.time()
-    samples, systems = dataset(a.n, a.seeds, cells=a.two_level)
+    samples, systems = dataset(a.n, a.seeds, probes=a.probes, cells=a.two_level)
     t1 = time.time()
     net = LR.MPNN(seed=1)
     if a.two_level:
@@ -98,6 +100,7 @@ def main():
     hist = LR.train(net, samples, epochs=a.epochs, lr=3e-3, batch=8)
     np.save(a.out, net.params())
     print(json.dumps({"n": a.n, "seeds": a.seeds, "two_level_cells": a.two_level,
+                      "probes": a.probes,
                       "systems": systems,
                       "samples": len(samples), "data_s": round(t1 - t0, 1),
                       "train_s": round(time.time() - t1, 1),
