@@ -30,6 +30,7 @@
 //     aggregate is empty; a pivot <= 0 is reported as an error);
 //   * restriction and the coarse product are warp sums in a fixed order.
 #include <math.h>
+#include <string.h>
 
 #include <algorithm>
 #include <functional>
@@ -293,11 +294,29 @@ int coarse_setup(gb300_matrix *A, const double *val, bool reuse)
       reinterpret_cast<unsigned long long *>(c->inv.p), c->err.p);
   k_coarse_to_double<<<grid_for(m, 256, kReduceBlocks), 256, 0, st>>>(m, c->headroom, amax,
                                                                       c->inv.p);
-  k_gj_init<<<grid_for(nc, 256), 256, 0, st>>>(nc, c->inv.p, c->rbuf.p, c->cbuf.p);
-  const int g = grid_for(m, 256, kReduceBlocks * 2);
-  for(int k = 0; k < nc; k++)
-    k_gj_step<<<g, 256, 0, st>>>(nc, k, c->inv.p, c->rbuf.p, c->cbuf.p, c->err.p);
   GB_CUDA(cudaGetLastError());
+  const void *key[4] = {c->inv.p, c->rbuf.p, c->cbuf.p, c->err.p};
+  if(!c->gj_exec || c->gj_nc != nc || memcmp(key, c->gj_key, sizeof(key)) != 0) {
+    if(c->gj_exec) cudaGraphExecDestroy(c->gj_exec);
+    c->gj_exec = nullptr;
+    cudaGraph_t graph;
+    GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    k_gj_init<<<grid_for(nc, 256), 256, 0, st>>>(nc, c->inv.p, c->rbuf.p, c->cbuf.p);
+    const int g = grid_for(m, 256, kReduceBlocks * 2);
+    for(int k = 0; k < nc; k++)
+      k_gj_step<<<g, 256, 0, st>>>(nc, k, c->inv.p, c->rbuf.p, c->cbuf.p, c->err.p);
+    GB_CUDA(cudaStreamEndCapture(st, &graph));
+    cudaError_t e = cudaGraphInstantiate(&c->gj_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if(e != cudaSuccess) {
+      c->gj_exec = nullptr;
+      set_error("coarse matrix: graph instantiation failed: %s", cudaGetErrorString(e));
+      return GB300_ERR_CUDA;
+    }
+    c->gj_nc = nc;
+    memcpy(c->gj_key, key, sizeof(key));
+  }
+  GB_CUDA(cudaGraphLaunch(c->gj_exec, st));
   int err = 0;
   GB_CUDA(cudaMemcpyAsync(&err, c->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));

@@ -87,6 +87,15 @@ struct Coarse {
   DevBuf<double> rc, ec;          // coarse residual and correction
   DevBuf<int> err;
   DevBuf<double> amax;
+  // the nc pivot launches of the inversion, captured once in a CUDA graph
+  // (replayed while nc and the buffers stay the same)
+  cudaGraphExec_t gj_exec = nullptr;
+  const void *gj_key[4] = {nullptr, nullptr, nullptr, nullptr};
+  int gj_nc = 0;
+  ~Coarse()
+  {
+    if(gj_exec) cudaGraphExecDestroy(gj_exec);
+  }
 };
 void coarse_free(Coarse *c);
 bool coarse_valid(const gb300_matrix *A);

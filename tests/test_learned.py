@@ -263,3 +263,43 @@ def test_committed_weights_fit_the_network():
     out = M.forward(w, g)
     assert np.all(np.isfinite(np.asarray(out[0] if isinstance(out, tuple) else out)))
     importlib.import_module("getdp_gb300.weights.train_nl2d")
+
+
+@pytest.mark.gpu
+def test_gpu_two_level_correction_reduces_steps_on_held_out_systems():
+    """The committed correction for the two-level cycle
+    (mpnn_nl2d_256_twolevel.npy, trained on Newton systems of seeds 200-364
+    at 256^2) on held-out systems of the same distribution (seeds 5, 6):
+    FGMRES with it (Preconditioner 22) takes fewer steps than the cycle
+    without it (21) and reaches the same solution.  It does not take less
+    time: the correction costs two more sparse products per smoothing."""
+    import os
+    G, LR, LA = _gpu()
+    wfile = os.path.join(os.path.dirname(LR.__file__), "weights",
+                         "mpnn_nl2d_256_twolevel.npy")
+    net = LR.MPNN(seed=1)
+    net.set_params(np.load(wfile))
+    for seed in (5, 6):
+        p = W.nonlinear_2d(n=256, seed=seed)
+        dm = W.dofmap_for(p)
+        terms = G.DeviceTerms(p, dm)
+        A, b = LA.gMatrix(dm.n_dof), LA.gVector(dm.n_dof)
+        G.generate(A, b, terms.batch, pattern=True)
+        agg, nc = W.cell_aggregates(p, dm, 8)
+        A.set_aggregates(agg, nc)
+        net.infer(A)
+        sols, steps = [], []
+        for prec in (21, 22):
+            S = LA.LinAlg_CreateSolver(None)
+            for k, v in dict(Algorithm=9, Preconditioner=prec, Krylov_Size=50,
+                             Nb_Iter_Max=2000, Renumbering_Technique=1, Precision=1).items():
+                S.set(k, v)
+            S["stopping_test"] = 1e-10
+            x = LA.gVector(dm.n_dof)
+            info = LA.LinAlg_Solve(A, b, S, x)
+            assert info["status"] == 0
+            sols.append(x.numpy())
+            steps.append(info["iterations"])
+        print(f"seed {seed}: two-level {steps[0]} steps, with the correction {steps[1]}")
+        assert steps[1] <= 0.95 * steps[0]
+        assert np.linalg.norm(sols[1] - sols[0]) <= 1e-6 * np.linalg.norm(sols[0])
