@@ -245,13 +245,14 @@ def test_gpu_step_length_and_newton_policy():
     assert all(k == "ilu0 (learned off)" for k in kinds[1:]), kinds
 
 
-def test_committed_weights_fit_the_network():
+@pytest.mark.parametrize("name", ["mpnn_nl2d_256.npy", "mpnn_nl2d_256_twolevel.npy"])
+def test_committed_weights_fit_the_network(name):
     # the weights that getdp_gb300/weights/train_nl2d.py produced: one
     # parameter vector of the network's layout, finite, with a non-zero head
     import os
     import importlib
     w = np.load(os.path.join(os.path.dirname(__file__), "..", "getdp_gb300", "weights",
-                             "mpnn_nl2d_256.npy"))
+                             name))
     assert w.dtype == np.float32 and w.shape == (M.NPARAM,)
     assert np.all(np.isfinite(w))
     assert np.any(w[M.OFF_WO:M.OFF_CO] != 0)  # trained: the output head moved off zero
