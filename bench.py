@@ -55,13 +55,14 @@ def parse():
                          "--size is the spelling torchrun passes through")
     ap.add_argument("--workload", default="elasticity",
                     choices=["elasticity", "magnetostatics2d", "curlcurl", "eddysweep",
-                             "nonlinear"],
+                             "nonlinear", "io"],
                     help="elasticity: 3D P2 elasticity, Jacobi-CG (the headline); "
                          "magnetostatics2d: 2D P1 a_z, ILU(0)-GMRES(50) to 1e-10; "
                          "curlcurl: 3D Whitney-edge curl-curl, ILU(0)-FGMRES(40) "
                          "to 1e-8, FP64 and FP32-ILU; eddysweep: 512 complex 2D "
                          "eddy-current problems of 32^2..160^2 cells in one batched "
-                         "Generate + batched ILU(0)-GMRES")
+                         "Generate + batched ILU(0)-GMRES; io: the host steps either "
+                         "side of the path (MSH 2.2 read, numbering, .pre/.res write)")
     ap.add_argument("--cpu-n", type=int, default=128,
                     help="nonlinear: mesh size of the CPU (oracle) comparison run")
     ap.add_argument("--problems", type=int, default=512,
@@ -819,9 +820,83 @@ def run_nonlinear(args, ws, rank, local):
         print(json.dumps(line))
 
 
+def run_io(args, ws, rank):
+    """The steps either side of the path, on the host: the MSH 2.2 reader
+    (native and numpy), DOF numbering and edge creation, and the .pre and
+    .res writers, as MB/s or unknowns/s on the largest configurations'
+    meshes.  Best of `steps` runs after `warmup`."""
+    from getdp_gb300 import fileio as FI
+    from getdp_gb300 import workloads as W
+
+    def best(f):
+        for _ in range(args.warmup):
+            f()
+        ts = []
+        for _ in range(max(args.steps, 1)):
+            t0 = time.perf_counter()
+            f()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    out = {}
+    tmp = tempfile.mkdtemp()
+    n = args.n or 1024
+    p = W.nonlinear_2d(n=n, seed=5)
+    msh = os.path.join(tmp, "m.msh")
+    W.write_msh22(p.mesh, msh)
+    mb = os.path.getsize(msh) / 1e6
+    t_nat = best(lambda: FI.read_msh22(msh))
+    t_np = best(lambda: FI.read_msh22_numpy(msh))
+    out["msh22_read"] = {"file_mb": round(mb, 1), "nodes": p.mesh.n_nodes,
+                         "elements": p.mesh.n_elems, "native_s": t_nat,
+                         "native_mb_s": mb / t_nat, "numpy_s": t_np, "numpy_mb_s": mb / t_np}
+    t_num = best(lambda: W.dofmap_for(p))
+    dm = W.dofmap_for(p)
+    out["dof_numbering_2d"] = {"unknowns": dm.n_dof, "s": t_num,
+                               "unknowns_per_s": dm.n_dof / t_num}
+    pre = os.path.join(tmp, "m.pre")
+    t_pre = best(lambda: FI.write_pre(pre, p.mesh, dm))
+    out["pre_write"] = {"mb": round(os.path.getsize(pre) / 1e6, 1), "s": t_pre,
+                        "mb_s": os.path.getsize(pre) / 1e6 / t_pre}
+    res = os.path.join(tmp, "m.res")
+    x = np.random.default_rng(0).standard_normal(dm.n_dof)
+    t_res = best(lambda: FI.write_res(res, x, binary=True))
+    out["res_write_binary"] = {"mb": round(os.path.getsize(res) / 1e6, 1), "s": t_res,
+                               "mb_s": os.path.getsize(res) / 1e6 / t_res}
+    e = W.elasticity_p2(n=48, seed=2)
+    t_e = best(lambda: W.dofmap_for(e))
+    ne = W.dofmap_for(e).n_dof
+    out["dof_numbering_p2_48"] = {"unknowns": ne, "s": t_e, "unknowns_per_s": ne / t_e}
+    c = W.curlcurl_edge(n=40, seed=3)
+    t_c = best(lambda: W.dofmap_for(c))
+    nc = W.dofmap_for(c).n_dof
+    out["edge_creation_numbering_40"] = {"unknowns": nc, "s": t_c, "unknowns_per_s": nc / t_c}
+    for f in (msh, pre, res):
+        os.remove(f)
+    os.rmdir(tmp)
+    line = {"metric": "host pre-processing and file formats: MSH 2.2 read, DOF numbering, "
+                      ".pre/.res write", "value": out["msh22_read"]["native_mb_s"],
+            "unit": "MB/s (MSH 2.2 read)", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "host", "data": "synthetic (seeded)",
+            "config": {"workload": f"nonlinear 2D mesh {n}^2x2 triangles (MSH 2.2 ASCII), "
+                                   "P2 elasticity 48^3, edge curl-curl 40^3"},
+            "gpu_launches": 0}
+    line.update(out)
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     args = parse()
     ws, rank, local, pg = dist_setup(args)
+    if args.workload == "io":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference arm times the headline workload only"}))
+            return
+        run_io(args, ws, rank)
+        return
     if args.workload == "nonlinear":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":

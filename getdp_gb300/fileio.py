@@ -249,8 +249,12 @@ def dof_records(mesh, dm):
         recs.append(np.stack([numtype, ent, np.full(len(d), h), np.where(unk, 1, 2),
                               num, val], 1))
     r = np.concatenate(recs)
-    key = r[:, :3].astype(np.int64)
-    _, first = np.unique(key, axis=0, return_index=True)
+    # (NumType, Entity, Harmonic) order as one integer key
+    ki = r[:, :3].astype(np.int64)
+    span_e = int(ki[:, 1].max()) + 1 if len(ki) else 1
+    span_h = int(ki[:, 2].max()) + 1 if len(ki) else 1
+    key = (ki[:, 0] * span_e + ki[:, 1]) * span_h + ki[:, 2]
+    _, first = np.unique(key, return_index=True)
     return r[first]
 
 
@@ -268,11 +272,11 @@ def write_pre(path: str, mesh, dm, resolution: str = "R", n_spaces: int = None) 
            "$DofData /* #0 */", "0 0",
            " ".join([str(n_spaces)] + [str(i) for i in range(n_spaces)]),
            "1 0", "1 0", f"{len(r)} {n_unknown}"]
-    for nt, ent, h, typ, num, val in r:
-        if int(typ) == 1:
-            out.append(f"{int(nt)} {int(ent)} {int(h)} 1 {int(num)} 1")
-        else:
-            out.append(f"{int(nt)} {int(ent)} {int(h)} 2 {'%.16g' % val} 0")
+    ints = r[:, :5].astype(np.int64).tolist()
+    vals = r[:, 5].tolist()
+    out.extend(f"{nt} {ent} {h} 1 {num} 1" if typ == 1 else
+               f"{nt} {ent} {h} 2 {'%.16g' % v} 0"
+               for (nt, ent, h, typ, num), v in zip(ints, vals))
     out.append("$EndDofData")
     if dm.edges is not None:
         out.extend(_elements_x_edges(mesh, dm))
@@ -303,8 +307,9 @@ def _elements_x_edges(mesh, dm):
     lines = ["$ElementsXEdges", f"0 {sum(len(b) for b in blocks)}"]
     i = 0
     for blk in blocks:
-        for row in blk:
-            lines.append(f"{i} {len(row)} " + " ".join(str(int(v)) for v in row))
+        w = blk.shape[1]
+        for row in blk.tolist():
+            lines.append(f"{i} {w} " + " ".join(map(str, row)))
             i += 1
     lines.append("$EndElementsXEdges")
     return lines
