@@ -3,6 +3,7 @@
 // element tables of the batched Generate.  Elements are kept grouped by
 // Gmsh type in file order; node references stay Gmsh node numbers.
 #include <cerrno>
+#include <charconv>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -65,11 +66,17 @@ struct Cursor {
   }
   double real()
   {
+    // bounded by the buffer's end and correctly rounded, like strtod on a
+    // terminated string (std::from_chars takes no leading '+')
     skip();
-    char *e = nullptr;
-    double v = strtod(p, &e);
-    if(e == p) ok = false;
-    p = e;
+    if(p < end && *p == '+') p++;
+    double v = 0.;
+    auto r = std::from_chars(p, end, v);
+    if(r.ec != std::errc() || r.ptr == p) {
+      ok = false;
+      return 0.;
+    }
+    p = r.ptr;
     return v;
   }
   bool line_starting(const char *tag)
