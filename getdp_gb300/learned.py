@@ -362,15 +362,15 @@ class TwoLevelNewtonSolver:
     which measured 7-9 on the nonlinear Jacobians and made FGMRES fail.
     The method without the network is the same cycle with plain ILU(0)
     smoothing (Preconditioner 21): it is used when the step is below
-    min_step, when the learned solve does not converge within the last
-    plain step count, and for good after max_failures such attempts; the
-    first solve runs it to set that count.  The FP64 residual decides in
+    min_step, when the learned solve does not converge within cap_margin
+    times the last plain step count, and for good after max_failures such
+    attempts; the first solve runs it to set that count.  The FP64 residual decides in
     every case."""
 
     def __init__(self, net: MPNN, agg, n_agg: int, stopping_test: float = 1e-10,
                  krylov: int = 50, nb_iter_max: int = 20000, precision: int = 1,
                  max_failures: int = 1, min_step: float = 0.05, step: float = 1.0,
-                 preconditioner: int = 22):
+                 preconditioner: int = 22, cap_margin: float = 1.25):
         self.net = net
         self.agg = np.ascontiguousarray(agg, np.int32)
         self.n_agg = int(n_agg)
@@ -382,6 +382,7 @@ class TwoLevelNewtonSolver:
         self.min_step = min_step
         self.step = step
         self.preconditioner = preconditioner  # 22, or 23: first smoothing only
+        self.cap_margin = cap_margin
         self.failures = 0
         self.last_plain = None
         self.seen = None
@@ -425,8 +426,11 @@ class TwoLevelNewtonSolver:
                 if omega != 1.0:
                     check(_lib.load().gb300_matrix_scale_correction(A.h,
                                                                     ctypes.c_double(omega)))
-                info = LA.LinAlg_Solve(A, b, self._params(self.preconditioner, self.last_plain),
-                                       x)
+                # Newton's later systems take more steps than the one that
+                # set the count: a quarter of margin before the attempt is
+                # called stagnant
+                cap = int(np.ceil(self.cap_margin * self.last_plain))
+                info = LA.LinAlg_Solve(A, b, self._params(self.preconditioner, cap), x)
                 info["preconditioner"] = "two-level learned"
                 info["step"] = omega
                 if info["status"] != 0:
