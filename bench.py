@@ -78,7 +78,8 @@ def parse():
     ap.add_argument("--profile-iterations", type=int, default=64)
     ap.add_argument("--coarse-cells", type=int, default=32,
                     help="nonlinear: cells per side of the aggregates of the two-level "
-                         "preconditioner (Preconditioner 21)")
+                         "preconditioner (Preconditioner 21); 0: aggregates from the "
+                         "matrix graph")
     ap.add_argument("--learned-two-level-weights", default=None,
                     help="nonlinear workload: also time the Newton loop with the correction "
                          "trained for the two-level cycle (Preconditioner 22, .npy)")
@@ -673,9 +674,12 @@ def run_nonlinear(args, ws, rank, local):
         """Preconditioner 21: the two-level cycle on cells of the mesh; the
         aggregates are handed to the matrix at its first solve (the host's
         counting sort is inside the timed loop)."""
-        agg, nc = W.cell_aggregates(p, dm, args.coarse_cells)
         S = params(prec)
         S.set("Preconditioner", 21)
+        if args.coarse_cells <= 0:
+            # no mesh given: the solver aggregates A's graph at its first solve
+            return S, "from the matrix graph"
+        agg, nc = W.cell_aggregates(p, dm, args.coarse_cells)
         seen = []
 
         def solve(A, b, x):

@@ -128,6 +128,7 @@ SIGNATURES = {
                              ctypes.POINTER(_I), ctypes.POINTER(_I), _PP, _PP, _PP]),
     "gb300_matrix_set_correction": (_I, [_P, _P, _I]),
     "gb300_matrix_set_aggregates": (_I, [_P, _P, _I]),
+    "gb300_matrix_aggregate_graph": (_I, [_P, _I]),
     "gb300_matrix_coarse_energy": (_I, [_P, _P, _P]),
     "gb300_matrix_scale_correction": (_I, [_P, ctypes.c_double]),
     "gb300_precond_apply": (_I, [_P, ctypes.POINTER(SolverParams), _P, _P]),

@@ -888,6 +888,17 @@ int gb300_matrix_set_aggregates(gb300_matrix *A, const int *agg, int n_agg)
   return coarse_set(A, agg, n_agg);
 }
 
+int gb300_matrix_aggregate_graph(gb300_matrix *A, int n_agg)
+{
+  GB_TRY(check(A, "matrix"));
+  GB_TRY(gb300_matrix_assemble(A));
+  if(n_agg < 1 || n_agg > kMaxCoarse) {
+    set_error("aggregates: %d aggregates asked (1 to %d supported)", n_agg, kMaxCoarse);
+    return GB300_ERR_ARG;
+  }
+  return coarse_auto(A, n_agg);
+}
+
 int gb300_matrix_coarse_energy(gb300_matrix *A, const gb300_vector *u, double *ucu)
 {
   GB_TRY(check(A, "matrix"));

@@ -897,6 +897,10 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
   else if(p->algorithm == 8 || p->algorithm == 9 ||
           (p->algorithm == 1 && (p->preconditioner == 6 ||
                                  p->preconditioner == kPrecondLearned))) {
+    // the two-level cycles without aggregates from the caller: from A's graph
+    if((p->preconditioner == kPrecondCoarse || p->preconditioner == kPrecondLearnedCoarse ||
+        p->preconditioner == kPrecondLearnedCoarsePre) && !coarse_valid(A))
+      GB_TRY(coarse_auto(A, std::min(kAutoAggregates, std::max(1, A->n / 16))));
     // Renumbering_Technique 1 (RCMK in Sparskit): this backend's own
     // renumbering, a multicolour ordering, for the ILU(0) solves
     bool used = false;

@@ -100,6 +100,9 @@ struct Coarse {
 void coarse_free(Coarse *c);
 bool coarse_valid(const gb300_matrix *A);
 int coarse_set(gb300_matrix *A, const int *agg, int nc);
+// aggregates of about n / target rows from A's graph (greedy breadth-first)
+int coarse_auto(gb300_matrix *A, int target);
+constexpr int kAutoAggregates = 1024;
 int coarse_follow(const gb300_matrix *A, gb300_matrix *B, const Colouring *C,
                   cudaStream_t st);
 int coarse_setup(gb300_matrix *A, const double *val, bool reuse);

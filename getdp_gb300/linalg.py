@@ -245,6 +245,10 @@ class gMatrix:
             n_agg = int(a.max()) + 1 if len(a) else 0
         check(_lib.load().gb300_matrix_set_aggregates(self.h, _ptr(a), int(n_agg)))
 
+    def aggregate_graph(self, n_agg: int = 1024) -> None:
+        """Aggregates from the matrix graph alone (no mesh needed)."""
+        check(_lib.load().gb300_matrix_aggregate_graph(self.h, int(n_agg)))
+
     def add_coo(self, i, j, v) -> None:
         i = np.ascontiguousarray(i, np.int32)
         j = np.ascontiguousarray(j, np.int32)

@@ -351,6 +351,11 @@ int gb300_matrix_scale_correction(gb300_matrix *A, double s);
    row; 1 <= n_agg <= 2048; a pattern change drops them.  A must be symmetric
    positive definite for Ac to be (a non-positive pivot of Ac is an error). */
 int gb300_matrix_set_aggregates(gb300_matrix *A, const int *agg, int n_agg);
+/* Aggregates from A's graph alone, about n / n_agg rows each (greedy
+   breadth-first over A's pattern, small leftovers joined to a neighbour);
+   a solve with Preconditioner 21-23 on a matrix without aggregates makes
+   them so, with n_agg = min(1024, n / 16). */
+int gb300_matrix_aggregate_graph(gb300_matrix *A, int n_agg);
 /* u^T P0 Ac^-1 P0^T u for A's aggregates and its own values (the part of
    the energy of an error e with A e = u that the coarse correction removes);
    the coarse inverse is made at the first call and then reused. */

@@ -162,10 +162,8 @@ def test_invalid_aggregates_are_errors():
         A.set_aggregates(np.zeros(n), 2)
     with pytest.raises(LA.GetDPError, match="supported"):
         A.set_aggregates(np.arange(n) % 3000, 3000)
-    # no aggregates: Preconditioner 21 reports it
-    x = LA.gVector(n)
-    with pytest.raises(LA.GetDPError, match="aggregates"):
-        LA.LinAlg_Solve(A, b, _params(21, 1), x)
+    with pytest.raises(LA.GetDPError, match="supported"):
+        A.aggregate_graph(0)
 
 
 def test_indefinite_coarse_matrix_is_an_error():
@@ -198,3 +196,24 @@ def test_zero_correction_gives_the_plain_cycle():
         assert i21["status"] == 0 and i22["status"] == 0
         assert i21["iterations"] == i22["iterations"]
         assert np.array_equal(x21, x22)
+
+
+def test_aggregates_from_the_matrix_graph():
+    # GetDP's solve has no mesh at hand: Preconditioner 21 on a matrix
+    # without aggregates makes them from A's graph, and they serve as well
+    p, dm, A, b, _ = _system(128, state_scale=0.02)
+    x1, i1 = _solve(A, b, _params(6, 1, stop=1e-12))
+    x2, i2 = _solve(A, b, _params(21, 1, stop=1e-12))   # aggregates made here
+    agg, nc = W.cell_aggregates(p, dm, 8)
+    A.set_aggregates(agg, nc)
+    x3, i3 = _solve(A, b, _params(21, 1, stop=1e-12))
+    print(f"ILU(0) {i1['iterations']}, graph aggregates {i2['iterations']}, "
+          f"cells {i3['iterations']}")
+    assert i1["status"] == 0 and i2["status"] == 0 and i3["status"] == 0
+    assert i2["iterations"] * 3 < i1["iterations"]
+    assert i2["iterations"] <= 1.25 * i3["iterations"]
+    assert np.linalg.norm(x2 - x1) <= 1e-7 * np.linalg.norm(x1)
+    # explicit: about n / 256 rows each
+    A.aggregate_graph(256)
+    x4, i4 = _solve(A, b, _params(21, 1, stop=1e-12))
+    assert i4["status"] == 0
