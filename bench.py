@@ -70,11 +70,13 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 comparison solve (profiling runs)")
-    ap.add_argument("--profile", choices=["spmv32", "spmv64", "generate", "step"],
+    ap.add_argument("--profile", choices=["spmv32", "spmv64", "generate", "step", "twolevel"],
                     help="minimal run for ncu: one Generate, then 3 warm-up "
                          "and 3 timed launches of the chosen kernel; 'step': "
                          "one warm-up step, then one Generate + mixed solve "
-                         "capped at --profile-iterations CG iterations")
+                         "capped at --profile-iterations CG iterations; "
+                         "'twolevel': nonlinear 2D magnetostatics, two solves "
+                         "with the two-level cycle")
     ap.add_argument("--profile-iterations", type=int, default=64)
     ap.add_argument("--coarse-cells", type=int, default=32,
                     help="nonlinear: cells per side of the aggregates of the two-level "
@@ -96,6 +98,28 @@ def profile_run(args):
     from getdp_gb300 import linalg as LA
     from getdp_gb300 import workloads as W
     L = _lib.load(build_if_missing=True)
+    if args.profile == "twolevel":
+        # nonlinear 2D magnetostatics at a = 0: one Generate, then two
+        # solves with the two-level cycle (the first makes the colouring,
+        # the aggregates and the graphs)
+        n = args.n or 1024
+        p = W.nonlinear_2d(n=n, seed=5)
+        dm = W.dofmap_for(p)
+        terms = G.DeviceTerms(p, dm)
+        A, b, x = LA.gMatrix(dm.n_dof), LA.gVector(dm.n_dof), LA.gVector(dm.n_dof)
+        G.generate(A, b, terms.batch, pattern=True)
+        agg, nc = W.cell_aggregates(p, dm, args.coarse_cells)
+        A.set_aggregates(agg, nc)
+        S = LA.LinAlg_CreateSolver(None)
+        for k, v in dict(Algorithm=8, Preconditioner=21, Krylov_Size=50, Nb_Iter_Max=20000,
+                         Renumbering_Technique=1).items():
+            S.set(k, v)
+        S["stopping_test"] = 1e-10
+        for _ in range(2):
+            info = LA.LinAlg_Solve(A, b, S, x)
+        print(json.dumps({"profile": "twolevel", "n": n, "aggregates": nc,
+                          "iterations": info["iterations"]}))
+        return
     p = W.elasticity_p2(n=args.n, seed=2)
     dm = W.dofmap_for(p)
     terms = G.DeviceTerms(p, dm)
