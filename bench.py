@@ -70,13 +70,15 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 comparison solve (profiling runs)")
-    ap.add_argument("--profile", choices=["spmv32", "spmv64", "generate", "step", "twolevel"],
+    ap.add_argument("--profile", choices=["spmv32", "spmv64", "generate", "step", "twolevel",
+                                          "mpnn"],
                     help="minimal run for ncu: one Generate, then 3 warm-up "
                          "and 3 timed launches of the chosen kernel; 'step': "
                          "one warm-up step, then one Generate + mixed solve "
                          "capped at --profile-iterations CG iterations; "
                          "'twolevel': nonlinear 2D magnetostatics, two solves "
-                         "with the two-level cycle")
+                         "with the two-level cycle; 'mpnn': three inferences of "
+                         "the learned correction on that system")
     ap.add_argument("--profile-iterations", type=int, default=64)
     ap.add_argument("--coarse-cells", type=int, default=32,
                     help="nonlinear: cells per side of the aggregates of the two-level "
@@ -98,6 +100,23 @@ def profile_run(args):
     from getdp_gb300 import linalg as LA
     from getdp_gb300 import workloads as W
     L = _lib.load(build_if_missing=True)
+    if args.profile == "mpnn":
+        # the learned correction's inference (3 message-passing layers and
+        # the output head) on the nonlinear 2D system at a = 0, three times
+        from getdp_gb300 import learned as LR
+        n = args.n or 1024
+        p = W.nonlinear_2d(n=n, seed=5)
+        dm = W.dofmap_for(p)
+        terms = G.DeviceTerms(p, dm)
+        A, b = LA.gMatrix(dm.n_dof), LA.gVector(dm.n_dof)
+        G.generate(A, b, terms.batch, pattern=True)
+        net = LR.MPNN(seed=1)
+        net.set_params(np.load(os.path.join(ROOT, "getdp_gb300", "weights",
+                                            "mpnn_nl2d_256_twolevel.npy")))
+        for _ in range(3):
+            net.infer(A)
+        print(json.dumps({"profile": "mpnn", "n": n, "nnz": A.nnz()}))
+        return
     if args.profile == "twolevel":
         # nonlinear 2D magnetostatics at a = 0: one Generate, then two
         # solves with the two-level cycle (the first makes the colouring,
