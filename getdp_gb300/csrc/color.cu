@@ -411,13 +411,10 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
 {
   cudaStream_t st = A->ctx->stream;
   const int n = A->n;
-  const bool learned = (p->preconditioner == kPrecondLearned ||
-                        p->preconditioner == kPrecondLearnedCoarse ||
-                        p->preconditioner == kPrecondLearnedCoarsePre);
-  const bool coarse = (p->preconditioner == kPrecondCoarse ||
-                       p->preconditioner == kPrecondLearnedCoarse ||
-                       p->preconditioner == kPrecondLearnedCoarsePre);
+  const bool learned = precond_learned(p->preconditioner);
+  const bool coarse = precond_two_level(p->preconditioner);
   const bool learned_post = learned && p->preconditioner != kPrecondLearnedCoarsePre;
+  const bool sai = (p->preconditioner == kPrecondLearnedSai);
   if(p->preconditioner != 6 && !learned && !coarse) {
     set_error("preconditioner apply: Preconditioner %d is not an ILU(0)", p->preconditioner);
     return GB300_ERR_UNSUPPORTED;
@@ -444,7 +441,7 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
   const double *vin = v;
   double *zout = z;
   Colouring *C = nullptr;
-  if(p->renumbering_technique == 1) {
+  if(p->renumbering_technique == 1 && !sai) {
     const int whole[2] = {0, n};
     int rc = colour_build(A, 1, whole);
     if(rc != GB300_OK && rc != GB300_ERR_UNSUPPORTED) return rc;
@@ -467,12 +464,16 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
   }
   int zr = 0;
   // Re_Use_LU: keep the factor of the previous call (same pattern)
-  GB_TRY(ilu_factor(M, M->val.p, fp32, &zr, p->re_use_lu != 0));
+  if(!sai) GB_TRY(ilu_factor(M, M->val.p, fp32, &zr, p->re_use_lu != 0));
   if(zr) {
     set_error("Zero pivot on line %d in ILU", zr);
     return GB300_ERR_ZERO_PIVOT;
   }
   auto smooth = [&](const double *vv, double *zz, bool corr) {
+    if(sai) {  // z = G v
+      spmv_guarded(M, M->corr.p, vv, zz, nullptr, st);
+      return;
+    }
     ilu_apply(M, fp32, vv, zz, fp32 ? t32.p : nullptr, nullptr, st);
     if(corr) correction_apply(M, M->val.p, vv, zz, t1.p, t2.p, nullptr, st);
   };

@@ -963,14 +963,12 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   }
   // 20: ILU(0) followed by the learned correction on A's pattern; 21, 22:
   // the two-level cycle on aggregates around ILU(0) (22: and the correction)
-  const bool learned = (p->preconditioner == kPrecondLearned ||
-                        p->preconditioner == kPrecondLearnedCoarse ||
-                        p->preconditioner == kPrecondLearnedCoarsePre);
-  const bool coarse = (p->preconditioner == kPrecondCoarse ||
-                       p->preconditioner == kPrecondLearnedCoarse ||
-                       p->preconditioner == kPrecondLearnedCoarsePre);
+  const bool learned = precond_learned(p->preconditioner);
+  const bool coarse = precond_two_level(p->preconditioner);
   const bool learned_post = learned && p->preconditioner != kPrecondLearnedCoarsePre;
-  bool precond = (p->preconditioner == 6) || learned || coarse;
+  // 24: G alone smooths, no ILU(0)
+  const bool sai = (p->preconditioner == kPrecondLearnedSai);
+  bool precond = ((p->preconditioner == 6) || learned || coarse) && !sai;
   if(p->preconditioner != 0 && p->preconditioner != 6 && p->preconditioner != 8 &&
      !learned && !coarse) {
     set_error("Preconditioner %d is not supported by this backend", p->preconditioner);
@@ -1032,6 +1030,10 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   // one-block reductions short); fixed for a given n, so deterministic
   const int nb = std::min(kReduceBlocks, std::max(152, (n + 2047) / 2048));
   auto smooth = [&](const double *v, double *z, const int *flag, bool corr) {
+    if(sai) {  // z = G v
+      spmv_guarded(A, A->corr.p, v, z, flag, st);
+      return;
+    }
     if(precond)
       ilu_apply(A, fp32, v, z, t32, flag, st);
     else

@@ -898,8 +898,7 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
           (p->algorithm == 1 && (p->preconditioner == 6 ||
                                  p->preconditioner == kPrecondLearned))) {
     // the two-level cycles without aggregates from the caller: from A's graph
-    if((p->preconditioner == kPrecondCoarse || p->preconditioner == kPrecondLearnedCoarse ||
-        p->preconditioner == kPrecondLearnedCoarsePre) && !coarse_valid(A))
+    if(precond_two_level(p->preconditioner) && !coarse_valid(A))
       GB_TRY(coarse_auto(A, std::min(kAutoAggregates, std::max(1, A->n / 16))));
     // Renumbering_Technique 1 (RCMK in Sparskit): this backend's own
     // renumbering, a multicolour ordering, for the ILU(0) solves
@@ -908,6 +907,7 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
        (p->preconditioner == 6 || p->preconditioner == kPrecondLearned ||
         p->preconditioner == kPrecondCoarse || p->preconditioner == kPrecondLearnedCoarse ||
         p->preconditioner == kPrecondLearnedCoarsePre)) {
+      // (24 has no triangular sweeps: it keeps GetDP's order)
       rc = gmres_solve_coloured(A, val, rhs, x, p, info, W, &used);
       if(rc != GB300_OK) return rc;
     }

@@ -73,6 +73,19 @@ constexpr int kPrecondLearnedCoarse = 22;
 // 23: as 22 with the correction in the first smoothing only (the half of
 // the cycle its loss is trained on; half its cost)
 constexpr int kPrecondLearnedCoarsePre = 23;
+// 24: the two-level cycle smoothed by the learned sparse approximate inverse
+// G alone (z = G v: one product per smoothing, no ILU(0) factor)
+constexpr int kPrecondLearnedSai = 24;
+inline bool precond_two_level(int p)
+{
+  return p == kPrecondCoarse || p == kPrecondLearnedCoarse || p == kPrecondLearnedCoarsePre ||
+         p == kPrecondLearnedSai;
+}
+inline bool precond_learned(int p)
+{
+  return p == kPrecondLearned || p == kPrecondLearnedCoarse || p == kPrecondLearnedCoarsePre ||
+         p == kPrecondLearnedSai;
+}
 constexpr int kMaxCoarse = 2048;  // dense coarse inverse: at most 32 MiB
 struct Coarse {
   int n = 0, nc = 0;

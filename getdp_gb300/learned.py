@@ -90,9 +90,10 @@ class Sample:
 
 
 def make_sample(A: LA.gMatrix, b: LA.gVector, x_star: LA.gVector,
-                renumbering: int = 1) -> Sample:
+                renumbering: int = 1, ilu: bool = True) -> Sample:
     """Training targets for one system: z1 = ILU^-1 b, r1 = b - A z1,
-    e1 = x* - z1 (all on the GPU)."""
+    e1 = x* - z1 (all on the GPU); without ilu, z1 = 0 (r1 = b, e1 = x*:
+    G then stands alone, as in Preconditioner 24)."""
     L = _lib.load()
     n = A.n
     z1 = LA.gVector(n)
@@ -100,7 +101,9 @@ def make_sample(A: LA.gMatrix, b: LA.gVector, x_star: LA.gVector,
     e1 = LA.gVector(n)
     b._flush()
     x_star._flush()
-    check(L.gb300_precond_apply(A.h, ctypes.byref(ilu_params(renumbering).params), b.h, z1.h))
+    if ilu:
+        check(L.gb300_precond_apply(A.h, ctypes.byref(ilu_params(renumbering).params),
+                                    b.h, z1.h))
     check(L.gb300_matrix_mult(A.h, z1.h, r1.h))          # r1 = A z1
     check(L.gb300_vector_axpby(1.0, b.h, -1.0, r1.h))     # r1 = b - A z1
     check(L.gb300_vector_axpby(1.0, x_star.h, 0.0, e1.h))
@@ -131,7 +134,8 @@ def make_probes(A: LA.gMatrix, count: int, seed: int, renumbering: int = 1) -> l
     return out
 
 
-def make_error_probes(A: LA.gMatrix, count: int, seed: int, renumbering: int = 1) -> list:
+def make_error_probes(A: LA.gMatrix, count: int, seed: int, renumbering: int = 1,
+                      ilu: bool = True) -> list:
     """Random probes with a known solution: e0 random, b = A e0, then as
     make_sample (z1 = ILU^-1 b, r1 = b - A z1 = A e1, e1 = e0 - z1), so
     that r1 = A e1 holds exactly, as the two-level loss needs."""
@@ -144,7 +148,7 @@ def make_error_probes(A: LA.gMatrix, count: int, seed: int, renumbering: int = 1
         e0._flush()
         b = LA.gVector(A.n)
         check(L.gb300_matrix_mult(A.h, e0.h, b.h))
-        out.append(make_sample(A, b, e0, renumbering))
+        out.append(make_sample(A, b, e0, renumbering, ilu))
     return out
 
 
@@ -381,7 +385,8 @@ class TwoLevelNewtonSolver:
         self.max_failures = max_failures
         self.min_step = min_step
         self.step = step
-        self.preconditioner = preconditioner  # 22, or 23: first smoothing only
+        # 22; 23: the correction in the first smoothing only; 24: G alone
+        self.preconditioner = preconditioner
         self.cap_margin = cap_margin
         self.failures = 0
         self.last_plain = None
@@ -390,7 +395,9 @@ class TwoLevelNewtonSolver:
 
     def _params(self, prec: int, cap: int) -> LA.gSolver:
         S = LA.LinAlg_CreateSolver(None)
-        for k, v in dict(Algorithm=9, Preconditioner=prec, Krylov_Size=self.krylov,
+        # 24 is a fixed linear operator (no FP32 factor): GMRES suffices
+        alg = 8 if prec == 24 else 9
+        for k, v in dict(Algorithm=alg, Preconditioner=prec, Krylov_Size=self.krylov,
                          Nb_Iter_Max=cap, Renumbering_Technique=1,
                          Precision=self.precision).items():
             S.set(k, v)
@@ -416,7 +423,7 @@ class TwoLevelNewtonSolver:
         else:
             self.net.infer(A)
             omega = self.step
-            if omega is None:
+            if omega is None and self.preconditioner != 24:
                 omega = step_length_two_level(A, precision=self.precision, rhs=b)
             if omega < self.min_step:
                 info = self._plain(A, b, x, "two-level ilu0 (correction rejected)",

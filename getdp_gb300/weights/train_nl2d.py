@@ -18,8 +18,12 @@ system carries those aggregates, the probes are random errors e0 with
 b = A e0 (so that r1 = A e1 exactly), and the loss is the energy of the
 error left after the coarse correction (gb300_mpnn_set_loss mode 1):
 
-    python -m getdp_gb300.weights.train_nl2d --n 256 --seeds 200 \
+    python -m getdp_gb300.weights.train_nl2d --n 256 --seeds 165 \
         --two-level 8 --out getdp_gb300/weights/mpnn_nl2d_256_twolevel.npy
+
+With --smoother g, G is trained to stand alone as the smoother of the
+cycle (Preconditioner 24: z = G v, no ILU(0)): the samples skip the ILU(0)
+step (r1 = b, e1 = x*).
 """
 from __future__ import annotations
 
@@ -48,7 +52,7 @@ def plain_fp64(precond: int = 6):
 
 
 def dataset(n: int, seeds: int, probes: int = 2, first_seed: int = 200,
-            cells: int = 0):
+            cells: int = 0, ilu: bool = True):
     """(samples, number of Newton systems among them); cells > 0: the
     systems carry aggregates of cells per side (two-level training)"""
     samples = []
@@ -68,10 +72,11 @@ def dataset(n: int, seeds: int, probes: int = 2, first_seed: int = 200,
             Ac, bc, xc = LR.copy_matrix(A), LR.copy_vector(b), LR.copy_vector(x)
             if cells:
                 Ac.set_aggregates(agg, nc)
-            samples.append(LR.make_sample(Ac, bc, xc))
+            samples.append(LR.make_sample(Ac, bc, xc, ilu=ilu))
             systems[0] += 1
             if cells:  # the two-level loss needs r1 = A e1 exactly
-                samples.extend(LR.make_error_probes(Ac, probes, seed=5000 + len(samples)))
+                samples.extend(LR.make_error_probes(Ac, probes, seed=5000 + len(samples),
+                                                    ilu=ilu))
             else:
                 samples.extend(LR.make_probes(Ac, probes, seed=5000 + len(samples)))
             return info
@@ -89,10 +94,14 @@ def main():
                     help="random probes per Newton system")
     ap.add_argument("--two-level", type=int, default=0, metavar="CELLS",
                     help="train for the two-level cycle on CELLS x CELLS aggregates")
+    ap.add_argument("--smoother", choices=["ilu", "g"], default="ilu",
+                    help="two-level: train G after the ILU(0) step (Preconditioner 22) "
+                         "or standing alone (24)")
     ap.add_argument("--out", required=True)
     a = ap.parse_args()
     t0 = time.time()
-    samples, systems = dataset(a.n, a.seeds, probes=a.probes, cells=a.two_level)
+    samples, systems = dataset(a.n, a.seeds, probes=a.probes, cells=a.two_level,
+                               ilu=a.smoother == "ilu")
     t1 = time.time()
     net = LR.MPNN(seed=1)
     if a.two_level:
@@ -100,7 +109,7 @@ def main():
     hist = LR.train(net, samples, epochs=a.epochs, lr=3e-3, batch=8)
     np.save(a.out, net.params())
     print(json.dumps({"n": a.n, "seeds": a.seeds, "two_level_cells": a.two_level,
-                      "probes": a.probes,
+                      "probes": a.probes, "smoother": a.smoother,
                       "systems": systems,
                       "samples": len(samples), "data_s": round(t1 - t0, 1),
                       "train_s": round(time.time() - t1, 1),
