@@ -259,17 +259,31 @@ def train(net: MPNN, samples: list, epochs: int = 20, lr: float = 3e-3,
     """Adam on mini-batches of systems; returns the mean loss per epoch."""
     rng = np.random.default_rng(seed)
     hist = []
+    skipped = [0]
     for _ in range(epochs):
         order = rng.permutation(len(samples))
         tot = 0.0
+        ep_used = 0
         for s0 in range(0, len(order), batch):
             idx = order[s0:s0 + batch]
-            for k, i in enumerate(idx):
+            used = 0
+            for i in idx:
+                ep_used += 1
                 s = samples[i]
-                loss, _ = net.loss_grad(s.A, s.r1, s.e1, accumulate=k > 0)
+                try:
+                    loss, _ = net.loss_grad(s.A, s.r1, s.e1, accumulate=used > 0)
+                except _lib.GetDPError:
+                    # a sample whose energy normalisation is not positive
+                    # (zero error): nothing to learn from it
+                    skipped[0] += 1
+                    ep_used -= 1
+                    continue
                 tot += loss
-            net.adam_step(lr, 1.0 / len(idx))
-        hist.append(tot / len(samples))
+                used += 1
+            if used:
+                net.adam_step(lr, 1.0 / used)
+        hist.append(tot / max(ep_used, 1))
+    net.skipped = skipped[0]
     return hist
 
 

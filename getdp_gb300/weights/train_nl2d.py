@@ -110,6 +110,7 @@ def main():
     np.save(a.out, net.params())
     print(json.dumps({"n": a.n, "seeds": a.seeds, "two_level_cells": a.two_level,
                       "probes": a.probes, "smoother": a.smoother,
+                      "skipped_per_run": getattr(net, "skipped", 0),
                       "systems": systems,
                       "samples": len(samples), "data_s": round(t1 - t0, 1),
                       "train_s": round(time.time() - t1, 1),
