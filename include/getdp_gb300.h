@@ -343,7 +343,8 @@ int gb300_matrix_scale_correction(gb300_matrix *A, double s);
    Preconditioners 21 and 22 (not Sparskit values) are a two-level cycle:
    z = S v; z += P0 Ac^-1 P0^T (v - A z); z += S (v - A z), with S = ILU(0)
    (21) or ILU(0) followed by the learned correction (22; 23: in the first
-   smoothing only), P0 the
+   smoothing only), or the learned sparse approximate inverse alone
+   (24: z = G v, no ILU(0) factor), P0 the
    piecewise-constant prolongation on aggregates of unknowns and
    Ac = P0^T A P0 inverted densely on the device at every solve (with
    Re_Use_LU, once).  gb300_matrix_set_aggregates gives the aggregate (0 ..
@@ -361,7 +362,7 @@ int gb300_matrix_aggregate_graph(gb300_matrix *A, int n_agg);
    the coarse inverse is made at the first call and then reused. */
 int gb300_matrix_coarse_energy(gb300_matrix *A, const gb300_vector *u, double *ucu);
 /* z = M^-1 v with the preconditioner the solver would use for p
-   (Preconditioner 6, 20, 21, 22 or 23; Renumbering_Technique selects the
+   (Preconditioner 6 or 20-24; Renumbering_Technique selects the
    ordering) on A's unscaled values; with p->re_use_lu the factor (and
    coarse inverse) of the previous call on A's pattern is kept. */
 int gb300_precond_apply(gb300_matrix *A, const gb300_solver_params *p,
