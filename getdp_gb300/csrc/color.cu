@@ -414,7 +414,8 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
   const bool learned = precond_learned(p->preconditioner);
   const bool coarse = precond_two_level(p->preconditioner);
   const bool learned_post = learned && p->preconditioner != kPrecondLearnedCoarsePre;
-  const bool sai = (p->preconditioner == kPrecondLearnedSai);
+  const bool sai = (p->preconditioner == kPrecondLearnedSai ||
+                    p->preconditioner == kPrecondSai);
   if(p->preconditioner != 6 && !learned && !coarse) {
     set_error("preconditioner apply: Preconditioner %d is not an ILU(0)", p->preconditioner);
     return GB300_ERR_UNSUPPORTED;
@@ -477,6 +478,7 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
     ilu_apply(M, fp32, vv, zz, fp32 ? t32.p : nullptr, nullptr, st);
     if(corr) correction_apply(M, M->val.p, vv, zz, t1.p, t2.p, nullptr, st);
   };
+  if(p->preconditioner == kPrecondSai) GB_TRY(spai1(M, M->val.p));
   if(coarse) {
     GB_TRY(coarse_setup(M, M->val.p, p->re_use_lu != 0));
     two_level_apply(M, M->val.p, vin, zout, t3.p, t4.p, nullptr, st,

@@ -966,8 +966,11 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
   const bool learned = precond_learned(p->preconditioner);
   const bool coarse = precond_two_level(p->preconditioner);
   const bool learned_post = learned && p->preconditioner != kPrecondLearnedCoarsePre;
-  // 24: G alone smooths, no ILU(0)
-  const bool sai = (p->preconditioner == kPrecondLearnedSai);
+  // 24: G alone smooths, no ILU(0); 25: with G the SPAI-1 made here
+  const bool sai = (p->preconditioner == kPrecondLearnedSai ||
+                    p->preconditioner == kPrecondSai);
+  if(p->preconditioner == kPrecondSai && !(p->re_use_lu && correction_valid(A)))
+    GB_TRY(spai1(A, val));
   bool precond = ((p->preconditioner == 6) || learned || coarse) && !sai;
   if(p->preconditioner != 0 && p->preconditioner != 6 && p->preconditioner != 8 &&
      !learned && !coarse) {

@@ -76,11 +76,15 @@ constexpr int kPrecondLearnedCoarsePre = 23;
 // 24: the two-level cycle smoothed by the learned sparse approximate inverse
 // G alone (z = G v: one product per smoothing, no ILU(0) factor)
 constexpr int kPrecondLearnedSai = 24;
+// 25: as 24 with G the SPAI-1 of A computed by the solver (spai.cu)
+constexpr int kPrecondSai = 25;
 inline bool precond_two_level(int p)
 {
   return p == kPrecondCoarse || p == kPrecondLearnedCoarse || p == kPrecondLearnedCoarsePre ||
-         p == kPrecondLearnedSai;
+         p == kPrecondLearnedSai || p == kPrecondSai;
 }
+// G = SPAI-1 of A on its pattern, into A->corr (A symmetric, rows <= 16)
+int spai1(gb300_matrix *A, const double *val);
 inline bool precond_learned(int p)
 {
   return p == kPrecondLearned || p == kPrecondLearnedCoarse || p == kPrecondLearnedCoarsePre ||

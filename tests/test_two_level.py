@@ -217,3 +217,54 @@ def test_aggregates_from_the_matrix_graph():
     A.aggregate_graph(256)
     x4, i4 = _solve(A, b, _params(21, 1, stop=1e-12))
     assert i4["status"] == 0
+
+
+def _spai1(Am):
+    """G with rows argmin ||e_i - A g|| over A's pattern of row i (numpy)."""
+    n = Am.shape[0]
+    Ac = Am.tocsc()
+    G = Am.copy().astype(np.float64).tolil()
+    for i in range(n):
+        J = Am.indices[Am.indptr[i]:Am.indptr[i + 1]]
+        sub = Ac[:, J].toarray()
+        e = np.zeros(n)
+        e[i] = 1.0
+        g, *_ = np.linalg.lstsq(sub, e, rcond=None)
+        for j, gj in zip(J, g):
+            G[i, j] = gj
+    return G.tocsr()
+
+
+def test_spai_cycle_matches_its_definition():
+    # Preconditioner 25: the cycle smoothed by z = G v, G the SPAI-1 of A on
+    # its own pattern, made on the device
+    p, dm, A, b, _ = _system(24, state_scale=0.02)
+    agg, nc = W.cell_aggregates(p, dm, 4)
+    A.set_aggregates(agg, nc)
+    ip, ix, dv = A.csr()
+    Am = sp.csr_matrix((dv, ix, ip), shape=(A.n, A.n))
+    Gm = _spai1(Am)
+    P = sp.csr_matrix((np.ones(A.n), (np.arange(A.n), agg)), shape=(A.n, nc))
+    Aci = np.linalg.inv((P.T @ Am @ P).toarray())
+    v = np.random.default_rng(2).standard_normal(A.n)
+    z = Gm @ v
+    z = z + P @ (Aci @ (P.T @ (v - Am @ z)))
+    z = z + Gm @ (v - Am @ z)
+    got = _apply(A, _params(25, 0), v)
+    err = np.linalg.norm(got - z) / np.linalg.norm(z)
+    assert err < 1e-9, err
+
+
+def test_spai_cycle_solves_to_the_oracle_solution():
+    p, dm, A, b, _ = _system(128, state_scale=0.02)
+    agg, nc = W.cell_aggregates(p, dm, 8)
+    A.set_aggregates(agg, nc)
+    ip, ix, dv = A.csr()
+    xo, st, _, _ = oracle.solve(ip, ix, dv, b.numpy(), algorithm=8, preconditioner=6,
+                                renumbering=0, krylov_size=50, nb_iter_max=20000,
+                                stopping_test=1e-14)
+    x25, i25 = _solve(A, b, _params(25, 0, stop=1e-14))
+    x21, i21 = _solve(A, b, _params(21, 1, stop=1e-14))
+    print(f"SPAI-1 cycle {i25['iterations']} steps, ILU(0) cycle {i21['iterations']}")
+    assert i25["status"] == 0
+    assert np.linalg.norm(x25 - xo) <= 1e-10 * np.linalg.norm(xo)
