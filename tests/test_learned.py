@@ -245,7 +245,8 @@ def test_gpu_step_length_and_newton_policy():
     assert all(k == "ilu0 (learned off)" for k in kinds[1:]), kinds
 
 
-@pytest.mark.parametrize("name", ["mpnn_nl2d_256.npy", "mpnn_nl2d_256_twolevel.npy"])
+@pytest.mark.parametrize("name", ["mpnn_nl2d_256.npy", "mpnn_nl2d_256_twolevel.npy",
+                                  "mpnn_nl2d_256_sai.npy"])
 def test_committed_weights_fit_the_network(name):
     # the weights that getdp_gb300/weights/train_nl2d.py produced: one
     # parameter vector of the network's layout, finite, with a non-zero head
