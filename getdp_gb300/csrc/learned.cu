@@ -188,6 +188,131 @@ k_mp_layer(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
   }
 }
 
+// The same layer with its dense part on the tensor cores (mma.sync
+// m16n8k16, BF16 in, FP32 accumulation).  The kernel above is bound by its
+// load/store pipe: every lane broadcasts its channel by shuffle and reads a
+// row of the two 32 x 32 weight matrices from shared memory, 64 of each per
+// node and layer for 64 FMAs.  Here a warp takes 16 nodes at a time: it sums
+// their messages as above (lane = channel) into a 16 x 64 shared tile
+// [h | m], then multiplies the tile by [W_s | W_n]^T held in registers as
+// BF16 MMA operands (the weights are BF16-rounded already: exact).  The
+// activations are FP32; each is split into three BF16 parts
+// (x = hi + mid + lo, each the BF16 rounding of what is left), so the three
+// MMAs per k-slice carry 24 bits of every activation and the layer matches
+// the FP32 form to FP32 rounding.
+__device__ __forceinline__ unsigned bf16x2(float a, float b)
+{
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);  // a in the low half
+  return *reinterpret_cast<unsigned *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const unsigned (&a)[4], unsigned b0,
+                                         unsigned b1)
+{
+  asm volatile(
+    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+    "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+    : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+    : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+constexpr int kMmaWarps = 8;  // 16-node tiles per 256-thread CTA at a time
+
+__global__ void __launch_bounds__(32 * kMmaWarps)
+k_mp_layer_mma(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
+               const float *__restrict__ ehat, const float *__restrict__ wl,
+               const float *__restrict__ hin, float *__restrict__ mout,
+               float *__restrict__ hout)
+{
+  __shared__ float X[kMmaWarps][16][2 * kH + 1];  // per warp: [h | m] of 16 nodes
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, tig = lane & 3;
+  // B operands: B[k][o] = W[o][k], W = [W_s | W_n] (32 x 64); k-slice kt,
+  // output tile nt: rows k = 16 kt + 2 tig + {0,1} (b0) and + 8 (b1), o = 8 nt + g
+  unsigned B0[4][4], B1[4][4];
+#pragma unroll
+  for(int kt = 0; kt < 4; kt++)
+#pragma unroll
+    for(int nt = 0; nt < 4; nt++) {
+      const int o = 8 * nt + g, k0 = 16 * kt + 2 * tig;
+      auto w = [&](int k) {
+        return k < kH ? wl[o * kH + k] : wl[kH * kH + o * kH + (k - kH)];
+      };
+      B0[kt][nt] = bf16x2(w(k0), w(k0 + 1));
+      B1[kt][nt] = bf16x2(w(k0 + 8), w(k0 + 9));
+    }
+  float bias[4][2];
+#pragma unroll
+  for(int nt = 0; nt < 4; nt++) {
+    bias[nt][0] = wl[2 * kH * kH + 8 * nt + 2 * tig];
+    bias[nt][1] = wl[2 * kH * kH + 8 * nt + 2 * tig + 1];
+  }
+  const int ntiles = (n + 15) / 16;
+  for(int t = blockIdx.x * kMmaWarps + warp; t < ntiles; t += gridDim.x * kMmaWarps) {
+    // messages of the tile's 16 nodes, lane = channel
+    for(int r = 0; r < 16; r++) {
+      const int i = 16 * t + r;
+      float hi = 0.f, mi = 0.f;
+      if(i < n) {
+        for(int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+          const int j = col[k];
+          if(j != i) mi += ehat[k] * hin[(size_t)j * kH + lane];
+        }
+        hi = hin[(size_t)i * kH + lane];
+        mout[(size_t)i * kH + lane] = mi;
+      }
+      X[warp][r][lane] = hi;
+      X[warp][r][kH + lane] = mi;
+    }
+    __syncwarp();
+    float C[4][4];
+#pragma unroll
+    for(int nt = 0; nt < 4; nt++) C[nt][0] = C[nt][1] = C[nt][2] = C[nt][3] = 0.f;
+#pragma unroll
+    for(int kt = 0; kt < 4; kt++) {
+      // this thread's 8 activations of the 16 x 16 slice kt
+      float x[8];
+      const int c0 = 16 * kt + 2 * tig;
+      x[0] = X[warp][g][c0];
+      x[1] = X[warp][g][c0 + 1];
+      x[2] = X[warp][g + 8][c0];
+      x[3] = X[warp][g + 8][c0 + 1];
+      x[4] = X[warp][g][c0 + 8];
+      x[5] = X[warp][g][c0 + 9];
+      x[6] = X[warp][g + 8][c0 + 8];
+      x[7] = X[warp][g + 8][c0 + 9];
+#pragma unroll
+      for(int part = 0; part < 3; part++) {
+        float y[8];
+#pragma unroll
+        for(int q = 0; q < 8; q++) {
+          y[q] = __bfloat162float(__float2bfloat16_rn(x[q]));
+          x[q] -= y[q];  // what the next part carries
+        }
+        const unsigned a[4] = {bf16x2(y[0], y[1]), bf16x2(y[2], y[3]), bf16x2(y[4], y[5]),
+                               bf16x2(y[6], y[7])};
+#pragma unroll
+        for(int nt = 0; nt < 4; nt++) mma_bf16(C[nt], a, B0[kt][nt], B1[kt][nt]);
+      }
+    }
+    __syncwarp();
+    // C[nt]: rows g (c0, c1) and g + 8 (c2, c3), outputs 8 nt + 2 tig + {0,1}
+    const int i0 = 16 * t + g, i1 = i0 + 8;
+#pragma unroll
+    for(int nt = 0; nt < 4; nt++) {
+      const int o = 8 * nt + 2 * tig;
+      if(i0 < n) {
+        hout[(size_t)i0 * kH + o] = fmaxf(C[nt][0] + bias[nt][0], 0.f);
+        hout[(size_t)i0 * kH + o + 1] = fmaxf(C[nt][1] + bias[nt][1], 0.f);
+      }
+      if(i1 < n) {
+        hout[(size_t)i1 * kH + o] = fmaxf(C[nt][2] + bias[nt][0], 0.f);
+        hout[(size_t)i1 * kH + o + 1] = fmaxf(C[nt][3] + bias[nt][1], 0.f);
+      }
+    }
+  }
+}
+
 // output head: G on A's pattern
 __global__ void __launch_bounds__(32 * kNodeWarps)
 k_mp_output(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
@@ -455,8 +580,9 @@ static int mp_forward(gb300_mpnn *net, const gb300_matrix *A)
   k_round_bf16<<<grid_for(kParams, 256), 256, 0, st>>>(kParams, net->w.p, net->wq.p);
   int grid = grid_for(n, kNodeWarps, kReduceBlocks);
   k_mp_input<<<grid, 32 * kNodeWarps, 0, st>>>(n, g.feat.p, net->wq.p, g.h.p);
+  const int gm = grid_for((n + 15) / 16, kMmaWarps, kReduceBlocks);
   for(int l = 0; l < kLayers; l++)
-    k_mp_layer<<<grid, 32 * kNodeWarps, 0, st>>>(
+    k_mp_layer_mma<<<gm, 32 * kMmaWarps, 0, st>>>(
       n, A->rowptr.p, A->col.p, g.ehat.p, net->wq.p + kOffLayer + l * kLayerSize,
       g.h.p + (size_t)l * n * kH, g.m.p + (size_t)l * n * kH,
       g.h.p + (size_t)(l + 1) * n * kH);
