@@ -562,11 +562,11 @@ def run_sweep(args, ws, rank, local):
     b = LA.gVector(N)
     x = LA.gVector(N)
 
-    def params(prec):
+    def params(prec, form=1):
         S = LA.LinAlg_CreateSolver(None)
         par = dict(Algorithm=8 if prec == 0 else 9, Preconditioner=6, Krylov_Size=40,
                    Stopping_Test=1e-10, Nb_Iter_Max=5000, Renumbering_Technique=1,
-                   Precision=prec)
+                   Precision=prec, Batch_Kernel=form)
         for k, v in par.items():
             S.set(k, v)
         S["stopping_test"] = 1e-10
@@ -582,8 +582,10 @@ def run_sweep(args, ws, rank, local):
 
     res = {}
     sols = {}
-    for prec in (0, 1):
-        S = params(prec)
+    # form 1: one launch, a thread-block cluster per system; form 0: one
+    # launch per Krylov kernel for all systems in step
+    for prec, form in ((0, 1), (1, 1), (0, 0), (1, 0)):
+        S = params(prec, form)
         for _ in range(args.warmup):
             G.generate(A, b, terms.batch, pattern=True)
             LA.LinAlg_SolveBatch(A, b, S, x, bt.offsets)
@@ -598,15 +600,16 @@ def run_sweep(args, ws, rank, local):
             ts += elapsed(1, 2)
         its = [d["iterations"] for d in infos]
         rel = [d["true_residual"] / max(d["rhs_norm"], 1e-300) for d in infos]
-        res[prec] = {"s": (tg + ts) / args.steps, "generate_s": tg / args.steps,
+        res[prec, form] = {"s": (tg + ts) / args.steps, "generate_s": tg / args.steps,
                      "solve_s": ts / args.steps,
                      "solves_per_s": len(probs) / ((tg + ts) / args.steps),
                      "converged": int(sum(d["status"] == 0 for d in infos)),
                      "iterations_min_median_max": [int(min(its)), int(np.median(its)),
                                                    int(max(its))],
-                     "max_true_rel_residual": float(max(rel))}
-        sols[prec] = x.numpy().copy()
-    best = res[1]
+                     "max_true_rel_residual": float(max(rel)),
+                     "one_launch_form": all(d["batch_form"] == 1 for d in infos)}
+        sols[prec, form] = x.numpy().copy()
+    best = res[1, 1]
     line = {"metric": "batched sweep: 512 complex eddy-current problems, solves/s "
                       "(Generate + Solve to 1e-10)",
             "value": best["solves_per_s"], "unit": "solves/s", "n_gpus": ws,
@@ -618,7 +621,11 @@ def run_sweep(args, ws, rank, local):
                                    "batched ILU(0)-(F)GMRES(40)",
                        "elements": bt.problem.mesh.n_elems, "unknowns": N,
                        "nnz": A.nnz(), "parallelism": f"replicas x{ws}"},
-            "fp64": res[0], "mixed": res[1]}
+            "fp64": res[0, 1], "mixed": res[1, 1],
+            "per_kernel_form": {"fp64": res[0, 0], "mixed": res[1, 0]},
+            "forms_max_rel_diff": max(
+                float(np.linalg.norm(sols[q, 1] - sols[q, 0]) /
+                      max(np.linalg.norm(sols[q, 0]), 1e-300)) for q in (0, 1))}
     if not args.skip_cpu and rank == 0:
         import oracle
         oracle.build()
@@ -639,7 +646,7 @@ def run_sweep(args, ws, rank, local):
             n_sample += dm.n_dof
             r0, r1 = bt.offsets[k], bt.offsets[k + 1]
             for prec in (0, 1):
-                xg = sols[prec][r0:r1]
+                xg = sols[prec, 1][r0:r1]
                 errs[prec].append(float(np.linalg.norm(xg - xo) / max(np.linalg.norm(xo), 1e-300)))
         total = t_cpu * N / max(n_sample, 1)
         line["per_problem_rel_error_vs_oracle"] = {"fp64_max": max(errs[0]),

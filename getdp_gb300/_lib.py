@@ -45,6 +45,7 @@ class SolverParams(ctypes.Structure):
         ("iterative_improvement", ctypes.c_int), ("nb_iter_max", ctypes.c_int),
         ("stopping_test", ctypes.c_double), ("precision", ctypes.c_int),
         ("inner_tolerance", ctypes.c_double), ("inner_iter_max", ctypes.c_int),
+        ("batch_kernel", ctypes.c_int),
     ]
 
 
@@ -53,7 +54,8 @@ class SolveInfo(ctypes.Structure):
                 ("residual_estimate", ctypes.c_double),
                 ("true_residual", ctypes.c_double), ("rhs_norm", ctypes.c_double),
                 ("refinement_steps", ctypes.c_int),
-                ("inner_iterations", ctypes.c_int), ("ilu_factorized", ctypes.c_int)]
+                ("inner_iterations", ctypes.c_int), ("ilu_factorized", ctypes.c_int),
+                ("batch_form", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

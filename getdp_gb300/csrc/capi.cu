@@ -184,6 +184,7 @@ void gb300_solver_params_default(gb300_solver_params *p)
   p->precision = 0;
   p->inner_tolerance = 0.3;
   p->inner_iter_max = 1000;
+  p->batch_kernel = 1;
 }
 
 struct ParamKey {
@@ -215,6 +216,7 @@ static const ParamKey kKeys[] = {
   PK("Precision", 0, precision),
   PK("Inner_Tolerance", 1, inner_tolerance),
   PK("Inner_Iter_Max", 0, inner_iter_max),
+  PK("Batch_Kernel", 0, batch_kernel),
 };
 #undef PK
 

@@ -24,6 +24,7 @@
 // than 98 % of ||w||^2), and both return an orthonormal basis to working
 // precision.
 #include <algorithm>
+#include <memory>
 
 #include "krylov.cuh"
 
@@ -65,6 +66,7 @@ struct ilu_data {
   DevBuf<float> lu32, inv32;
   bool fact64 = false, fact32 = false;  // a factor of that precision is held
   unsigned version = ~0u;               // the matrix pattern it was set up for
+  std::unique_ptr<SysLevels> sys;       // the schedule cut into a batch's blocks
 };
 
 void ilu_free(ilu_data *d) { delete d; }
@@ -579,6 +581,93 @@ void ilu_apply(const gb300_matrix *A, bool fp32, const double *v, double *z,
                          nullptr, flag, st, rmask);
     k_cvt<double, float><<<grid_for(n, 256), 256, 0, st>>>(n, t32, z, flag);
   }
+}
+
+// one sweep's levels cut into the diagonal blocks off[0..nsys]: the rows of
+// each level go, in level order, to their system's range of out, and each
+// system records where its levels begin (a system's rows occupy the same
+// range [off[p], off[p+1]) in out as in the matrix)
+static void cut_levels(int n, int nsys, const int *off, const std::vector<int> &rows,
+                       const std::vector<int> &lptr, std::vector<int> &out,
+                       std::vector<int> &lev, std::vector<int> &lb, int *max_levels)
+{
+  std::vector<int> sys_of(n), fill(nsys), last(nsys, -1);
+  std::vector<std::vector<int>> starts(nsys);
+  for(int q = 0; q < nsys; q++) {
+    fill[q] = off[q];
+    for(int i = off[q]; i < off[q + 1]; i++) sys_of[i] = q;
+  }
+  out.assign(n, 0);
+  const int nl = (int)lptr.size() - 1;
+  for(int l = 0; l < nl; l++)
+    for(int t = lptr[l]; t < lptr[l + 1]; t++) {
+      int i = rows[t], q = sys_of[i];
+      if(last[q] != l) {
+        starts[q].push_back(fill[q]);
+        last[q] = l;
+      }
+      out[fill[q]++] = i;
+    }
+  lev.clear();
+  lb.assign(nsys + 1, 0);
+  for(int q = 0; q < nsys; q++) {
+    lb[q] = (int)lev.size();
+    lev.insert(lev.end(), starts[q].begin(), starts[q].end());
+    lev.push_back(off[q + 1]);
+    *max_levels = std::max(*max_levels, (int)starts[q].size());
+  }
+  lb[nsys] = (int)lev.size();
+}
+
+int ilu_sys_levels(gb300_matrix *A, int nsys, const int *off, const SysLevels **out)
+{
+  GB_TRY(ilu_setup(A));
+  ilu_data *L = A->ilu;
+  if(L->sys && (int)L->sys->off.size() == nsys + 1 &&
+     std::equal(off, off + nsys + 1, L->sys->off.begin())) {
+    *out = L->sys.get();
+    return GB300_OK;
+  }
+  cudaStream_t st = A->ctx->stream;
+  const int n = A->n;
+  std::vector<int> lr(n), ur(n);
+  if(n > 0) {
+    GB_CUDA(cudaMemcpyAsync(lr.data(), L->lrows.p, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemcpyAsync(ur.data(), L->urows.p, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+  }
+  GB_CUDA(cudaStreamSynchronize(st));
+  auto S = std::make_unique<SysLevels>();
+  S->off.assign(off, off + nsys + 1);
+  std::vector<int> lo, uo, llev, ulev, llb, ulb;
+  cut_levels(n, nsys, off, lr, L->hlptr, lo, llev, llb, &S->max_levels);
+  cut_levels(n, nsys, off, ur, L->huptr, uo, ulev, ulb, &S->max_levels);
+  auto up = [&](DevBuf<int> &d, const std::vector<int> &h) -> int {
+    GB_TRY(d.alloc(h.size() > 0 ? h.size() : 1));
+    if(!h.empty())
+      GB_CUDA(cudaMemcpyAsync(d.p, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice, st));
+    return GB300_OK;
+  };
+  GB_TRY(up(S->lrows, lo));
+  GB_TRY(up(S->urows, uo));
+  GB_TRY(up(S->llev, llev));
+  GB_TRY(up(S->ulev, ulev));
+  GB_TRY(up(S->llb, llb));
+  GB_TRY(up(S->ulb, ulb));
+  GB_CUDA(cudaStreamSynchronize(st));  // the host vectors go out of scope
+  L->sys = std::move(S);
+  *out = L->sys.get();
+  return GB300_OK;
+}
+
+// the factor held for A (after ilu_factor): values, inverted pivots and the
+// position of each diagonal entry
+void ilu_factor_arrays(const gb300_matrix *A, bool fp32, const void **lu, const void **inv,
+                       const int **diag)
+{
+  const ilu_data *L = A->ilu;
+  *lu = fp32 ? (const void *)L->lu32.p : (const void *)L->lu64.p;
+  *inv = fp32 ? (const void *)L->inv32.p : (const void *)L->inv64.p;
+  *diag = L->diag.p;
 }
 
 // ---------------------------------------------------------------------------

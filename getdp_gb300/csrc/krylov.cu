@@ -1028,11 +1028,16 @@ int solve_batch(gb300_matrix *A, const gb300_vector *bvec,
     GB_TRY(rb.alloc(n));
     GB_TRY(yb.alloc(n));
     permute_system(C, A->nnz, val, rhs, B->val.p, rb.p, st);
-    GB_TRY(gmres_solve_batch(B, B->val.p, rb.p, yb.p, p, nsys, off, infos, W));
+    bool used = false;
+    GB_TRY(gmres_solve_batch_cluster(B, B->val.p, rb.p, yb.p, p, nsys, off, infos, W, &used));
+    if(!used) GB_TRY(gmres_solve_batch(B, B->val.p, rb.p, yb.p, p, nsys, off, infos, W));
     unpermute_solution(C, yb.p, x, st);
   }
-  else
-    GB_TRY(gmres_solve_batch(A, val, rhs, x, p, nsys, off, infos, W));
+  else {
+    bool used = false;
+    GB_TRY(gmres_solve_batch_cluster(A, val, rhs, x, p, nsys, off, infos, W, &used));
+    if(!used) GB_TRY(gmres_solve_batch(A, val, rhs, x, p, nsys, off, infos, W));
+  }
   if(scaled) k_mul<<<grid_for(n, 256), 256, 0, st>>>(n, x, s.p, x);
   GB_CUDA(cudaGetLastError());
   GB_CUDA(cudaStreamSynchronize(st));

@@ -190,6 +190,30 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
 int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
                       double *x, const gb300_solver_params *p, int nsys,
                       const int *off, gb300_solve_info *infos, Work &W);
+
+// The ILU(0) level schedule cut into the diagonal blocks of a batch: system
+// p's rows are lrows[off[p] .. off[p+1]) grouped by forward-sweep level, its
+// levels bounded by llev[llb[p] .. llb[p+1]] (positions in lrows, so
+// llb[p+1] - llb[p] - 1 levels); the same for the backward sweep (u*).
+struct SysLevels {
+  std::vector<int> off;  // the block offsets it was made for
+  DevBuf<int> lrows, urows, llev, ulev, llb, ulb;
+  int max_levels = 0;    // most levels of one system in either sweep
+};
+// made (once per pattern and offsets) from A's ILU(0) schedule (gmres.cu)
+int ilu_sys_levels(gb300_matrix *A, int nsys, const int *off, const SysLevels **out);
+// the ILU(0) factor held for A after ilu_factor: values (double or float),
+// inverted pivots and the position of each row's diagonal entry
+void ilu_factor_arrays(const gb300_matrix *A, bool fp32, const void **lu, const void **inv,
+                       const int **diag);
+
+// batched GMRES/FGMRES with one thread-block cluster per system and the
+// whole solve in one launch (gmres_cluster.cu); *used is false, and nothing
+// is done, where that form does not apply (then gmres_solve_batch does)
+int gmres_solve_batch_cluster(gb300_matrix *A, const double *val, const double *rhs,
+                              double *x, const gb300_solver_params *p, int nsys,
+                              const int *off, gb300_solve_info *infos, Work &W,
+                              bool *used);
 int check_blocks(const gb300_matrix *A, int nsys, const int *off);
 
 // multicolour ordering of a pattern for the ILU(0) solves (color.cu)

@@ -61,7 +61,7 @@ int gb300_copy_to_host(gb300_ctx *ctx, void *dst, const void *src, size_t bytes)
    defaults (contrib/Sparskit/Sparskit.h:83-103 Solver_Params,
    Sparskit.cpp:1847-1868 Tab_Params).  Codes: Algorithm 1 CG, 8 GMRES,
    9 FGMRES; Preconditioner 0 none, 6 ILU0, 8 DIAGONAL; Scaling 0 none,
-   1 diagonal (D^-1/2 A D^-1/2).  The last three fields are extensions of
+   1 diagonal (D^-1/2 A D^-1/2).  The last four fields are extensions of
    this backend (keys Sparskit would reject as unknown). */
 typedef struct gb300_solver_params {
   int matrix_format;
@@ -89,6 +89,13 @@ typedef struct gb300_solver_params {
                              residual between two FP64 residual replacements
                              (default 0.3) */
   int inner_iter_max;     /* Inner_Iter_Max */
+  int batch_kernel;       /* Batch_Kernel: form of gb300_solve_batch: 1 (default)
+                             one launch for the whole batch, a thread-block
+                             cluster per system (GMRES/FGMRES, Krylov_Size
+                             <= 64, at most 64 ILU(0) levels per system, e.g.
+                             Renumbering_Technique 1); 0, or where 1 does not
+                             apply: one launch per Krylov kernel for all
+                             systems in step */
 } gb300_solver_params;
 
 /* Replaces Sparskit's init_solver defaults (Sparskit.cpp:1847-1868). */
@@ -116,6 +123,9 @@ typedef struct gb300_solve_info {
   int ilu_factorized;    /* 1: this solve computed an ILU(0) factorisation;
                             0: none, or the previous one was reused
                             (Re_Use_LU, as LinAlg_SolveAgain sets it) */
+  int batch_form;        /* gb300_solve_batch: 1 the one-launch form (a
+                            thread-block cluster per system) ran, 0 the
+                            per-kernel form; 0 for single solves */
 } gb300_solve_info;
 
 /* ---- vectors (device resident, FP64) -------------------------------- */

@@ -158,3 +158,99 @@ def test_batched_rejects_coupled_blocks_and_bad_offsets():
     off[-1] -= 1
     with pytest.raises(GetDPError, match="offsets"):
         LA.LinAlg_SolveBatch(A, b, _solver(LA, par), x, off)
+
+
+# ------------------------------------------ one launch, a cluster per system
+def _solve_form(LA, A, b, bt, par, form):
+    x = LA.gVector(bt.dofmap.n_dof)
+    S = _solver(LA, dict(par, Batch_Kernel=form))
+    infos = LA.LinAlg_SolveBatch(A, b, S, x, bt.offsets)
+    return infos, x.numpy()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("algorithm,precision,renumbering",
+                         [(8, 0, 1), (9, 0, 1), (9, 1, 1), (8, 1, 1), (9, 0, 0)])
+def test_cluster_form_follows_the_per_kernel_form(algorithm, precision, renumbering):
+    # the same iteration per system: step counts within 1 (the sums are
+    # formed in another order), solutions within rounding of the reductions
+    probs, bt, A, b, LA = _gpu_setup()
+    par = {"Algorithm": algorithm, "Preconditioner": 6, "Krylov_Size": 20,
+           "Renumbering_Technique": renumbering, "Stopping_Test": "1e-12",
+           "Nb_Iter_Max": 3000, "Precision": precision}
+    i1, x1 = _solve_form(LA, A, b, bt, par, 1)
+    i0, x0 = _solve_form(LA, A, b, bt, par, 0)
+    for k in range(len(probs)):
+        assert i1[k]["batch_form"] == 1 and i0[k]["batch_form"] == 0
+        assert i1[k]["status"] == 0 and i0[k]["status"] == 0, (k, i1[k], i0[k])
+        assert abs(i1[k]["iterations"] - i0[k]["iterations"]) <= 1, (k, i1[k], i0[k])
+        r0, r1 = bt.offsets[k], bt.offsets[k + 1]
+        assert np.linalg.norm(x1[r0:r1] - x0[r0:r1]) <= 1e-9 * np.linalg.norm(x0[r0:r1])
+        assert i1[k]["true_residual"] <= 1.01e-12 * i1[k]["rhs_norm"] or \
+            i1[k]["true_residual"] <= 2 * i0[k]["true_residual"], (k, i1[k], i0[k])
+
+
+@pytest.mark.gpu
+def test_cluster_form_uneven_sizes_against_oracle():
+    # more systems than clusters fit at once, sizes 3x3 to 30x30 cells,
+    # taken from the queue largest first; each against the oracle alone
+    oracle.build()
+    from getdp_gb300 import generate as G_
+    from getdp_gb300 import linalg as LA
+    probs = W.eddy_sweep(n_problems=48, seed=11, n_min=3, n_max=30)
+    bt = W.concat_problems(probs)
+    A = LA.gMatrix(bt.dofmap.n_dof)
+    b = LA.gVector(bt.dofmap.n_dof)
+    terms = G_.DeviceTerms(bt.problem, bt.dofmap)
+    G_.generate(A, b, terms.batch, pattern=True)
+    par = {"Algorithm": 9, "Preconditioner": 6, "Krylov_Size": 30,
+           "Renumbering_Technique": 1, "Stopping_Test": "1e-14", "Nb_Iter_Max": 5000}
+    infos, xs = _solve_form(LA, A, b, bt, par, 1)
+    assert all(d["batch_form"] == 1 and d["status"] == 0 for d in infos), infos
+    for k in (0, 7, 19, 33, 47):
+        oip, oix, odv, ob = oracle.assemble(probs[k], bt.dofmaps[k])
+        xo, st, its, _ = oracle.solve(oip, oix, odv, ob, algorithm=9, preconditioner=6,
+                                      renumbering=1, krylov_size=30,
+                                      stopping_test=float(np.float32(1e-14)),
+                                      nb_iter_max=5000)
+        assert st == 0
+        xk = xs[bt.offsets[k]:bt.offsets[k + 1]]
+        assert np.linalg.norm(xk - xo) <= 1e-10 * np.linalg.norm(xo), k
+
+
+@pytest.mark.gpu
+def test_cluster_form_without_preconditioner_and_at_the_iteration_cap():
+    probs, bt, A, b, LA = _gpu_setup()
+    # without a preconditioner some of these systems stagnate (GMRES(15)):
+    # both forms end the same way, converged or at the cap
+    par = {"Algorithm": 8, "Preconditioner": 0, "Krylov_Size": 15,
+           "Renumbering_Technique": 1, "Stopping_Test": "1e-10", "Nb_Iter_Max": 800}
+    i1, x1 = _solve_form(LA, A, b, bt, par, 1)
+    i0, x0 = _solve_form(LA, A, b, bt, par, 0)
+    for k in range(len(probs)):
+        assert i1[k]["batch_form"] == 1
+        assert i1[k]["status"] == i0[k]["status"], (k, i1[k], i0[k])
+        assert abs(i1[k]["iterations"] - i0[k]["iterations"]) <= 0.05 * i0[k]["iterations"] + 2
+        if i0[k]["status"] != 0:
+            assert abs(i1[k]["residual_estimate"] - i0[k]["residual_estimate"]) <= \
+                1e-6 * i0[k]["residual_estimate"], (k, i1[k], i0[k])
+    # a cap every system reaches: status -1 and the cap's product count, as
+    # the per-kernel form reports them (a warning, as LinAlg_Solve gives)
+    capped = dict(par, Nb_Iter_Max=7)
+    i1, x1 = _solve_form(LA, A, b, bt, capped, 1)
+    i0, x0 = _solve_form(LA, A, b, bt, capped, 0)
+    for k in range(len(probs)):
+        assert i1[k]["status"] == i0[k]["status"] == -1
+        assert "terminated" in i1[k]["warning"]
+        assert i1[k]["iterations"] == i0[k]["iterations"]
+        r0, r1 = bt.offsets[k], bt.offsets[k + 1]
+        assert np.linalg.norm(x1[r0:r1] - x0[r0:r1]) <= 1e-10 * np.linalg.norm(x0[r0:r1])
+
+
+@pytest.mark.gpu
+def test_cluster_form_falls_back_beyond_its_krylov_size():
+    probs, bt, A, b, LA = _gpu_setup()
+    par = {"Algorithm": 9, "Preconditioner": 6, "Krylov_Size": 80,
+           "Renumbering_Technique": 1, "Stopping_Test": "1e-10", "Nb_Iter_Max": 2000}
+    infos, _ = _solve_form(LA, A, b, bt, par, 1)
+    assert all(d["batch_form"] == 0 and d["status"] == 0 for d in infos)
