@@ -184,7 +184,7 @@ void gb300_solver_params_default(gb300_solver_params *p)
   p->precision = 0;
   p->inner_tolerance = 0.3;
   p->inner_iter_max = 1000;
-  p->batch_kernel = 1;
+  p->batch_kernel = 4;
 }
 
 struct ParamKey {

@@ -3,7 +3,7 @@
 //
 // The systems of a batch (the diagonal blocks of one matrix, as in
 // gmres_batch.cu) are independent, so nothing has to cross from one system
-// to another while they iterate: a cluster of kCCtas CTAs (on as many SMs)
+// to another while they iterate: a cluster of 1 to 16 CTAs (on as many SMs)
 // takes a system from a queue (largest first), runs its restart cycles and
 // Arnoldi steps to the end, and takes the next.  Within a cluster the rows
 // are split between the CTAs; the steps that need rows of other CTAs (the
@@ -43,7 +43,13 @@ namespace cg = cooperative_groups;
 
 namespace gb {
 
-constexpr int kCCtas = 8;  // CTAs per cluster (the portable cluster size)
+// CTAs per cluster (one cluster per system): Batch_Kernel 1, 2, 4, 8 (the
+// portable maximum) or 16 (a non-portable size this GPU allows).  Measured
+// on 512 complex systems of 1,922..51,842 rows (ILU(0)-GMRES(40), FP64 /
+// FP32 factor): 1 CTA 2.47 / 2.40 s, 2 1.41 / 1.37, 4 1.11 / 1.06, 8 1.31 /
+// 1.26, 16 1.89 / 1.75, against 1.19 / 1.23 s for the per-kernel form: few
+// CTAs leave the largest systems' steps to one or two SMs, many CTAs leave
+// fewer systems running at once and make each cluster barrier dearer
 constexpr int kCThreads = 512;
 constexpr int kCWarps = kCThreads / 32;
 constexpr int kCMaxKrylov = 64;
@@ -77,6 +83,7 @@ struct CArgs {
 
 // the sums over the cluster's CTAs, in rank order, of the nv partials each
 // CTA left in buf: every CTA gets the same values in out
+template <int CS>
 __device__ __forceinline__ void cluster_sum(cg::cluster_group &cl, double *buf, int nv,
                                             double *out)
 {
@@ -84,10 +91,43 @@ __device__ __forceinline__ void cluster_sum(cg::cluster_group &cl, double *buf, 
   for(int j = threadIdx.x; j < nv; j += kCThreads) {
     double s = 0.;
 #pragma unroll
-    for(int r = 0; r < kCCtas; r++) s += cl.map_shared_rank(buf, r)[j];
+    for(int r = 0; r < CS; r++) s += cl.map_shared_rank(buf, r)[j];
     out[j] = s;
   }
   __syncthreads();
+}
+
+// s - sum_k a[k] x[col[k]] over k = k0, k0 + step, ... < k1, in that order
+// (lusol's and amux's accumulation order), with the column indices and
+// values of up to eight entries loaded before their gathers, so that a
+// thread has eight loads in flight instead of a chain of dependent ones
+template <int STEP, bool SUB, typename T, typename X>
+__device__ __forceinline__ T row_acc(int k0, int k1, const int *__restrict__ col,
+                                     const T *__restrict__ a, const X *x, T s)
+{
+  for(int kb = k0; kb < k1; kb += 4 * STEP) {
+    int c[4];
+    T v[4];
+    X xv[4];
+#pragma unroll
+    for(int u = 0; u < 4; u++) {
+      int k = kb + u * STEP;
+      c[u] = k < k1 ? col[k] : 0;
+      v[u] = k < k1 ? a[k] : (T)0;
+    }
+#pragma unroll
+    for(int u = 0; u < 4; u++)
+      if(kb + u * STEP < k1) xv[u] = __ldcg(x + c[u]);
+#pragma unroll
+    for(int u = 0; u < 4; u++)
+      if(kb + u * STEP < k1) {
+        if(SUB)
+          s = s - v[u] * xv[u];
+        else
+          s += v[u] * xv[u];
+      }
+  }
+  return s;
 }
 
 // w = A z on the rows [lo, hi) (two lanes per row, as k_b_spmv); with RES,
@@ -100,9 +140,7 @@ __device__ __forceinline__ double c_spmv(const CArgs &P, int lo, int hi, const d
   double acc = 0., accb = 0.;
   for(int i = lo + sub; i - sub < hi; i += kCThreads / 2) {
     double s = 0.;
-    if(i < hi)
-      for(int k = P.rowptr[i] + l2; k < P.rowptr[i + 1]; k += 2)
-        s += P.val[k] * __ldcg(z + P.col[k]);
+    if(i < hi) s = row_acc<2, false>(P.rowptr[i] + l2, P.rowptr[i + 1], P.col, P.val, z, s);
     s += __shfl_down_sync(0xffffffffu, s, 1, 2);
     if(l2 == 0 && i < hi) {
       if(RES) {
@@ -162,7 +200,7 @@ __device__ __forceinline__ double c_update(const CArgs &P, int lo, int hi, doubl
 // level's rows split over the cluster (a barrier after each level), or a
 // copy without a preconditioner.  src must be complete (all CTAs) on entry;
 // dst is complete on return.
-template <typename T>
+template <typename T, int CS>
 __device__ void c_precond(const CArgs &P, cg::cluster_group &cl, int p, int rank, int lo,
                           int hi, const double *src, double *dst)
 {
@@ -175,39 +213,35 @@ __device__ void c_precond(const CArgs &P, cg::cluster_group &cl, int p, int rank
   cl.sync();  // src written by every CTA
   for(int l = P.llb[p]; l + 1 < P.llb[p + 1]; l++) {
     const int a = P.llev[l], cnt = P.llev[l + 1] - a;
-    const int t0 = a + (int)((long long)cnt * rank / kCCtas);
-    const int t1 = a + (int)((long long)cnt * (rank + 1) / kCCtas);
+    const int t0 = a + (int)((long long)cnt * rank / CS);
+    const int t1 = a + (int)((long long)cnt * (rank + 1) / CS);
     for(int t = t0 + threadIdx.x; t < t1; t += kCThreads) {
       const int i = P.lrows[t];
       const int ke = P.diag[i];
-      if constexpr(sizeof(T) == 8) {
-        double s = __ldcg(src + i);
-        for(int k = P.rowptr[i]; k < ke; k++) s = s - lu[k] * __ldcg(dst + P.col[k]);
-        dst[i] = s;
-      }
-      else {
-        float s = (float)__ldcg(src + i);
-        for(int k = P.rowptr[i]; k < ke; k++) s = s - lu[k] * __ldcg(P.t32 + P.col[k]);
-        P.t32[i] = s;
-      }
+      if constexpr(sizeof(T) == 8)
+        dst[i] = row_acc<1, true>(P.rowptr[i], ke, P.col, lu, (const double *)dst,
+                                  __ldcg(src + i));
+      else
+        P.t32[i] = row_acc<1, true>(P.rowptr[i], ke, P.col, lu, (const float *)P.t32,
+                                    (float)__ldcg(src + i));
     }
     cl.sync();
   }
   for(int l = P.ulb[p]; l + 1 < P.ulb[p + 1]; l++) {
     const int a = P.ulev[l], cnt = P.ulev[l + 1] - a;
-    const int t0 = a + (int)((long long)cnt * rank / kCCtas);
-    const int t1 = a + (int)((long long)cnt * (rank + 1) / kCCtas);
+    const int t0 = a + (int)((long long)cnt * rank / CS);
+    const int t1 = a + (int)((long long)cnt * (rank + 1) / CS);
     for(int t = t0 + threadIdx.x; t < t1; t += kCThreads) {
       const int i = P.urows[t];
       const int ke = P.rowptr[i + 1];
       if constexpr(sizeof(T) == 8) {
-        double s = __ldcg(dst + i);
-        for(int k = P.diag[i] + 1; k < ke; k++) s = s - lu[k] * __ldcg(dst + P.col[k]);
+        double s = row_acc<1, true>(P.diag[i] + 1, ke, P.col, lu, (const double *)dst,
+                                    __ldcg(dst + i));
         dst[i] = inv[i] * s;
       }
       else {
-        float s = __ldcg(P.t32 + i);
-        for(int k = P.diag[i] + 1; k < ke; k++) s = s - lu[k] * __ldcg(P.t32 + P.col[k]);
+        float s = row_acc<1, true>(P.diag[i] + 1, ke, P.col, lu, (const float *)P.t32,
+                                   __ldcg(P.t32 + i));
         float v = inv[i] * s;
         P.t32[i] = v;
         dst[i] = (double)v;
@@ -217,7 +251,7 @@ __device__ void c_precond(const CArgs &P, cg::cluster_group &cl, int p, int rank
   }
 }
 
-template <typename T>
+template <typename T, int CS>
 __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
 {
   cg::cluster_group cl = cg::this_cluster();
@@ -240,8 +274,8 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
     if(q >= P.nsys) break;
     const int p = P.order[q];
     const int r0 = P.off[p], np = P.off[p + 1] - r0;
-    const int lo = r0 + (int)((long long)np * rank / kCCtas);
-    const int hi = r0 + (int)((long long)np * (rank + 1) / kCCtas);
+    const int lo = r0 + (int)((long long)np * rank / CS);
+    const int hi = r0 + (int)((long long)np * (rank + 1) / CS);
     if(tid == 0) {
       memset(&S, 0, sizeof(S));
       S.active = 1;
@@ -257,7 +291,7 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
         double rr = c_spmv<1>(P, lo, hi, P.x, P.Vb, nullptr);
         rr = block_sum<double, kCThreads>(rr);
         if(tid == 0) xbuf[xb][0] = rr;
-        cluster_sum(cl, xbuf[xb], 1, sdot);
+        cluster_sum<CS>(cl, xbuf[xb], 1, sdot);
         xb ^= 1;
       }
       if(tid == 0) {
@@ -292,12 +326,12 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
         double *vk = P.Vb + (size_t)(k - 1) * P.ldv;
         double *w = P.Vb + (size_t)k * P.ldv;
         double *z = P.flexible ? P.Z + (size_t)(k - 1) * P.ldv : P.zt;
-        c_precond<T>(P, cl, p, rank, lo, hi, vk, z);
+        c_precond<T, CS>(P, cl, p, rank, lo, hi, vk, z);
         c_spmv<0>(P, lo, hi, z, w, nullptr);
         __syncthreads();
         // first Gram-Schmidt pass: <V_j, w> for j < k and <w, w>
         c_dots(P, lo, hi, w, k + 1, xbuf[xb]);
-        cluster_sum(cl, xbuf[xb], k + 1, sdot);
+        cluster_sum<CS>(cl, xbuf[xb], k + 1, sdot);
         xb ^= 1;
         if(tid == 0) {
           S.nrm0 = sdot[k];
@@ -321,7 +355,7 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
           double v = c_update(P, lo, hi, w, sh1, k);
           v = block_sum<double, kCThreads>(v);
           if(tid == 0) xbuf[xb][0] = v;
-          cluster_sum(cl, xbuf[xb], 1, sdot);
+          cluster_sum<CS>(cl, xbuf[xb], 1, sdot);
           xb ^= 1;
         }
         if(tid == 0) {
@@ -332,7 +366,7 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
         if(S.reorth) {
           // second pass
           c_dots(P, lo, hi, w, k, xbuf[xb]);
-          cluster_sum(cl, xbuf[xb], k, sdot);
+          cluster_sum<CS>(cl, xbuf[xb], k, sdot);
           xb ^= 1;
           if(tid == 0)
             for(int j = 0; j < k; j++) sH[(k - 1) * (m + 1) + j] = sh1[j] + sdot[j];
@@ -340,7 +374,7 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
           double v = c_update(P, lo, hi, w, sdot, k);
           v = block_sum<double, kCThreads>(v);
           if(tid == 0) xbuf[xb][0] = v;
-          cluster_sum(cl, xbuf[xb], 1, sdot);
+          cluster_sum<CS>(cl, xbuf[xb], 1, sdot);
           xb ^= 1;
           if(tid == 0) S.rr = sdot[0];
           __syncthreads();
@@ -426,7 +460,7 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
             for(int j = 0; j < k; j++) s += sy[j] * __ldcg(P.Vb + (size_t)j * P.ldv + i);
             P.u[i] = s;
           }
-          c_precond<T>(P, cl, p, rank, lo, hi, P.u, P.zt);
+          c_precond<T, CS>(P, cl, p, rank, lo, hi, P.u, P.zt);
           for(int i = lo + tid; i < hi; i += kCThreads) P.x[i] += __ldcg(P.zt + i);
         }
       }
@@ -465,7 +499,7 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
         xbuf[xb][0] = rr;
         xbuf[xb][1] = bb;
       }
-      cluster_sum(cl, xbuf[xb], 2, sdot);
+      cluster_sum<CS>(cl, xbuf[xb], 2, sdot);
       xb ^= 1;
     }
     if(rank == 0 && tid == 0) {
@@ -479,22 +513,30 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
   }
 }
 
-template <typename T> static int launch_c(const CArgs &a, cudaStream_t st, int *nclusters)
+template <typename T, int CS>
+static int launch_c(const CArgs &a, cudaStream_t st, int *nclusters)
 {
+  if(CS > 8 &&
+     cudaFuncSetAttribute(k_c_solve<T, CS>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                          1) != cudaSuccess) {
+    cudaGetLastError();
+    *nclusters = 0;
+    return GB300_OK;
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kCCtas;
+  attr[0].val.clusterDim.x = CS;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.blockDim = dim3(kCThreads, 1, 1);
   cfg.dynamicSmemBytes = 0;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cfg.gridDim = dim3(kCCtas, 1, 1);
+  cfg.gridDim = dim3(CS, 1, 1);
   int nc = 0;
-  cudaError_t e = cudaOccupancyMaxActiveClusters(&nc, (void *)k_c_solve<T>, &cfg);
+  cudaError_t e = cudaOccupancyMaxActiveClusters(&nc, (void *)k_c_solve<T, CS>, &cfg);
   if(e != cudaSuccess || nc < 1) {
     cudaGetLastError();
     *nclusters = 0;
@@ -502,8 +544,8 @@ template <typename T> static int launch_c(const CArgs &a, cudaStream_t st, int *
   }
   if(nc > a.nsys) nc = a.nsys;
   *nclusters = nc;
-  cfg.gridDim = dim3((unsigned)(nc * kCCtas), 1, 1);
-  if(cudaLaunchKernelEx(&cfg, k_c_solve<T>, a) != cudaSuccess) {
+  cfg.gridDim = dim3((unsigned)(nc * CS), 1, 1);
+  if(cudaLaunchKernelEx(&cfg, k_c_solve<T, CS>, a) != cudaSuccess) {
     // a launch the device refuses (nothing ran): the per-kernel form runs
     cudaGetLastError();
     *nclusters = 0;
@@ -517,7 +559,8 @@ int gmres_solve_batch_cluster(gb300_matrix *A, const double *val, const double *
                               bool *used)
 {
   *used = false;
-  if(p->batch_kernel != 1) return GB300_OK;
+  const int cs = p->batch_kernel;
+  if(cs != 1 && cs != 2 && cs != 4 && cs != 8 && cs != 16) return GB300_OK;
   if((p->algorithm != 8 && p->algorithm != 9) ||
      (p->preconditioner != 0 && p->preconditioner != 6))
     return GB300_OK;
@@ -609,7 +652,17 @@ int gmres_solve_batch_cluster(gb300_matrix *A, const double *val, const double *
   a.out_rr = dbl.p + nsys;
   a.out_bb = dbl.p + 2 * (size_t)nsys;
   int nc = 0;
-  GB_TRY((precond && fp32) ? launch_c<float>(a, st, &nc) : launch_c<double>(a, st, &nc));
+  const bool f32 = precond && fp32;
+#define GB_LAUNCH_C(CSZ)                                                              \
+  GB_TRY(f32 ? launch_c<float, CSZ>(a, st, &nc) : launch_c<double, CSZ>(a, st, &nc))
+  switch(cs) {
+  case 1: GB_LAUNCH_C(1); break;
+  case 2: GB_LAUNCH_C(2); break;
+  case 4: GB_LAUNCH_C(4); break;
+  case 8: GB_LAUNCH_C(8); break;
+  default: GB_LAUNCH_C(16); break;
+  }
+#undef GB_LAUNCH_C
   // no cluster fits or the launch was refused: nothing ran (x was zeroed, as
   // the per-kernel form does first), and that form solves instead
   if(nc < 1) return GB300_OK;

@@ -89,13 +89,14 @@ typedef struct gb300_solver_params {
                              residual between two FP64 residual replacements
                              (default 0.3) */
   int inner_iter_max;     /* Inner_Iter_Max */
-  int batch_kernel;       /* Batch_Kernel: form of gb300_solve_batch: 1 (default)
-                             one launch for the whole batch, a thread-block
-                             cluster per system (GMRES/FGMRES, Krylov_Size
-                             <= 64, at most 64 ILU(0) levels per system, e.g.
-                             Renumbering_Technique 1); 0, or where 1 does not
-                             apply: one launch per Krylov kernel for all
-                             systems in step */
+  int batch_kernel;       /* Batch_Kernel: form of gb300_solve_batch: c = 1, 2,
+                             4 (default), 8 or 16: one launch for the whole
+                             batch, a thread-block cluster of c CTAs per
+                             system (GMRES/FGMRES, Nb_Iter_Max > 0,
+                             Krylov_Size <= 64, at most 64 ILU(0) levels per
+                             system, e.g. Renumbering_Technique 1); 0, or
+                             where that does not apply: one launch per Krylov
+                             kernel for all systems in step */
 } gb300_solver_params;
 
 /* Replaces Sparskit's init_solver defaults (Sparskit.cpp:1847-1868). */

@@ -178,16 +178,17 @@ def test_cluster_form_follows_the_per_kernel_form(algorithm, precision, renumber
     par = {"Algorithm": algorithm, "Preconditioner": 6, "Krylov_Size": 20,
            "Renumbering_Technique": renumbering, "Stopping_Test": "1e-12",
            "Nb_Iter_Max": 3000, "Precision": precision}
-    i1, x1 = _solve_form(LA, A, b, bt, par, 1)
     i0, x0 = _solve_form(LA, A, b, bt, par, 0)
-    for k in range(len(probs)):
-        assert i1[k]["batch_form"] == 1 and i0[k]["batch_form"] == 0
-        assert i1[k]["status"] == 0 and i0[k]["status"] == 0, (k, i1[k], i0[k])
-        assert abs(i1[k]["iterations"] - i0[k]["iterations"]) <= 1, (k, i1[k], i0[k])
-        r0, r1 = bt.offsets[k], bt.offsets[k + 1]
-        assert np.linalg.norm(x1[r0:r1] - x0[r0:r1]) <= 1e-9 * np.linalg.norm(x0[r0:r1])
-        assert i1[k]["true_residual"] <= 1.01e-12 * i1[k]["rhs_norm"] or \
-            i1[k]["true_residual"] <= 2 * i0[k]["true_residual"], (k, i1[k], i0[k])
+    for form in (1, 2, 4, 8, 16):  # clusters of 1 to 16 CTAs
+        i1, x1 = _solve_form(LA, A, b, bt, par, form)
+        for k in range(len(probs)):
+            assert i1[k]["batch_form"] == 1 and i0[k]["batch_form"] == 0
+            assert i1[k]["status"] == 0 and i0[k]["status"] == 0, (k, i1[k], i0[k])
+            assert abs(i1[k]["iterations"] - i0[k]["iterations"]) <= 1, (k, i1[k], i0[k])
+            r0, r1 = bt.offsets[k], bt.offsets[k + 1]
+            assert np.linalg.norm(x1[r0:r1] - x0[r0:r1]) <= 1e-9 * np.linalg.norm(x0[r0:r1])
+            assert i1[k]["true_residual"] <= 1.01e-12 * i1[k]["rhs_norm"] or \
+                i1[k]["true_residual"] <= 2 * i0[k]["true_residual"], (k, i1[k], i0[k])
 
 
 @pytest.mark.gpu
@@ -205,7 +206,7 @@ def test_cluster_form_uneven_sizes_against_oracle():
     G_.generate(A, b, terms.batch, pattern=True)
     par = {"Algorithm": 9, "Preconditioner": 6, "Krylov_Size": 30,
            "Renumbering_Technique": 1, "Stopping_Test": "1e-14", "Nb_Iter_Max": 5000}
-    infos, xs = _solve_form(LA, A, b, bt, par, 1)
+    infos, xs = _solve_form(LA, A, b, bt, par, 4)
     assert all(d["batch_form"] == 1 and d["status"] == 0 for d in infos), infos
     for k in (0, 7, 19, 33, 47):
         oip, oix, odv, ob = oracle.assemble(probs[k], bt.dofmaps[k])
@@ -225,7 +226,7 @@ def test_cluster_form_without_preconditioner_and_at_the_iteration_cap():
     # both forms end the same way, converged or at the cap
     par = {"Algorithm": 8, "Preconditioner": 0, "Krylov_Size": 15,
            "Renumbering_Technique": 1, "Stopping_Test": "1e-10", "Nb_Iter_Max": 800}
-    i1, x1 = _solve_form(LA, A, b, bt, par, 1)
+    i1, x1 = _solve_form(LA, A, b, bt, par, 4)
     i0, x0 = _solve_form(LA, A, b, bt, par, 0)
     for k in range(len(probs)):
         assert i1[k]["batch_form"] == 1
@@ -237,7 +238,7 @@ def test_cluster_form_without_preconditioner_and_at_the_iteration_cap():
     # a cap every system reaches: status -1 and the cap's product count, as
     # the per-kernel form reports them (a warning, as LinAlg_Solve gives)
     capped = dict(par, Nb_Iter_Max=7)
-    i1, x1 = _solve_form(LA, A, b, bt, capped, 1)
+    i1, x1 = _solve_form(LA, A, b, bt, capped, 4)
     i0, x0 = _solve_form(LA, A, b, bt, capped, 0)
     for k in range(len(probs)):
         assert i1[k]["status"] == i0[k]["status"] == -1
@@ -252,5 +253,5 @@ def test_cluster_form_falls_back_beyond_its_krylov_size():
     probs, bt, A, b, LA = _gpu_setup()
     par = {"Algorithm": 9, "Preconditioner": 6, "Krylov_Size": 80,
            "Renumbering_Technique": 1, "Stopping_Test": "1e-10", "Nb_Iter_Max": 2000}
-    infos, _ = _solve_form(LA, A, b, bt, par, 1)
+    infos, _ = _solve_form(LA, A, b, bt, par, 4)
     assert all(d["batch_form"] == 0 and d["status"] == 0 for d in infos)
