@@ -277,6 +277,126 @@ k_bsr_spmv(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
   }
 }
 
+// Column indices one step ahead: in k_bsr_spmv a lane waits for a block's
+// column index before it can gather x, then for the gather, so each group
+// of blocks costs two memory latencies.  Here the column indices of a
+// lane's next UNR blocks are loaded while the current blocks' values and x
+// gathers are in flight (their columns were loaded the step before), and
+// the next block row's bounds while the current row runs: one latency per
+// group of blocks.  Same arithmetic and order as k_bsr_spmv.
+template <int MODE, typename T, int LPR, int UNR, int MINB = 0>
+__global__ void __launch_bounds__(256, MINB)
+k_bsr_spmv_pf(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
+              const T *__restrict__ val, long long nblk, const T *__restrict__ p,
+              const T *__restrict__ bvec, T *__restrict__ y,
+              double *__restrict__ part, const int *flag, double *dot_out,
+              unsigned *counter)
+{
+  if(flag && !*flag) return;
+  const int rows_per_block = 256 / LPR;
+  const long long stride = (long long)gridDim.x * rows_per_block;
+  int lane = threadIdx.x % LPR, sub = threadIdx.x / LPR;
+  typename Acc<T>::type red = 0;
+  long long a0 = (long long)blockIdx.x * rows_per_block;
+  int s = 0, e = 0;
+  if(a0 + sub < nn) {
+    s = __ldg(ptr + a0 + sub);
+    e = __ldg(ptr + a0 + sub + 1);
+  }
+  for(; a0 < nn; a0 += stride) {
+    long long a = a0 + sub;
+    // the next row's bounds
+    int sn = 0, en = 0;
+    if(a + stride < nn) {
+      sn = __ldg(ptr + a + stride);
+      en = __ldg(ptr + a + stride + 1);
+    }
+    T y0 = 0, y1 = 0, y2 = 0;
+    if(a < nn) {
+      int k = s + lane;
+      int c[UNR];
+#pragma unroll
+      for(int u = 0; u < UNR; u++) {
+        int kk = k + u * LPR;
+        c[u] = kk < e ? __ldg(col + kk) : 0;
+      }
+      for(; k < e; k += UNR * LPR) {
+        int cn[UNR];
+#pragma unroll
+        for(int u = 0; u < UNR; u++) {
+          int kk = k + (UNR + u) * LPR;
+          cn[u] = kk < e ? __ldg(col + kk) : 0;
+        }
+#pragma unroll
+        for(int u = 0; u < UNR; u++) {
+          int kk = k + u * LPR;
+          if(kk < e) {
+            auto xb = Vec4<T>::load(p + 4 * (size_t)c[u]);
+            if constexpr(sizeof(T) == 8) {
+              y0 = fma(__ldg(val + kk), xb.x, y0);
+              y1 = fma(__ldg(val + 3 * nblk + kk), xb.x, y1);
+              y2 = fma(__ldg(val + 6 * nblk + kk), xb.x, y2);
+              y0 = fma(__ldg(val + nblk + kk), xb.y, y0);
+              y1 = fma(__ldg(val + 4 * nblk + kk), xb.y, y1);
+              y2 = fma(__ldg(val + 7 * nblk + kk), xb.y, y2);
+              y0 = fma(__ldg(val + 2 * nblk + kk), xb.z, y0);
+              y1 = fma(__ldg(val + 5 * nblk + kk), xb.z, y1);
+              y2 = fma(__ldg(val + 8 * nblk + kk), xb.z, y2);
+            }
+            else {
+              y0 += __ldg(val + kk) * xb.x + __ldg(val + nblk + kk) * xb.y +
+                    __ldg(val + 2 * nblk + kk) * xb.z;
+              y1 += __ldg(val + 3 * nblk + kk) * xb.x + __ldg(val + 4 * nblk + kk) * xb.y +
+                    __ldg(val + 5 * nblk + kk) * xb.z;
+              y2 += __ldg(val + 6 * nblk + kk) * xb.x + __ldg(val + 7 * nblk + kk) * xb.y +
+                    __ldg(val + 8 * nblk + kk) * xb.z;
+            }
+          }
+        }
+#pragma unroll
+        for(int u = 0; u < UNR; u++) c[u] = cn[u];
+      }
+    }
+    s = sn;
+    e = en;
+#pragma unroll
+    for(int o = LPR / 2; o > 0; o >>= 1) {
+      y0 += __shfl_down_sync(0xffffffffu, y0, o, LPR);
+      y1 += __shfl_down_sync(0xffffffffu, y1, o, LPR);
+      y2 += __shfl_down_sync(0xffffffffu, y2, o, LPR);
+    }
+    if(lane == 0 && a < nn) {
+      size_t o = 4 * (size_t)a;
+      if(MODE == 1) {
+        T r0 = bvec[o] - y0, r1 = bvec[o + 1] - y1, r2 = bvec[o + 2] - y2;
+        y[o] = r0;
+        y[o + 1] = r1;
+        y[o + 2] = r2;
+        y[o + 3] = 0;
+        red += r0 * r0 + r1 * r1 + r2 * r2;
+      }
+      else {
+        y[o] = y0;
+        y[o + 1] = y1;
+        y[o + 2] = y2;
+        y[o + 3] = 0;
+        if(MODE == 2) red += p[o] * y0 + p[o + 1] * y1 + p[o + 2] * y2;
+      }
+    }
+  }
+  if(MODE != 0) {
+    double sm = block_sum<double, 256>((double)red);
+    if(threadIdx.x == 0) part[blockIdx.x] = sm;
+    if(blockIdx.x == 0)
+      for(int b = gridDim.x + threadIdx.x; b < kReduceBlocks; b += blockDim.x)
+        part[b] = 0.;
+    if(MODE == 2 && dot_out && arrive_last(counter)) {
+      double d = sum_partials_l2<256>(part);
+      if(threadIdx.x == 0) *dot_out = d;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // TMA-staged variant: each CTA walks tiles of kTileRows block rows; one
 // elected thread copies a tile's nine value planes and column indices from
@@ -517,8 +637,10 @@ k_bsr_spmv_tma(int nn, const int *__restrict__ ptr, const int *__restrict__ col,
 // 6 and 7: the TMA-staged kernel with 16 and 8 lanes per block row;
 // 8 (8,2,ldg,8 CTAs) 9 (8,4,ldg,4 CTAs) 10 (8,2,ldg,4 CTAs); fewer lanes
 // per block row, for the FP64 product whose shuffle-add tree and idle lanes
-// load GB300's FP64 pipe: 11 (4,2,ldg) 12 (4,4,ldg) 13 (2,4,ldg)
-constexpr int kBsrVariants = 14;
+// load GB300's FP64 pipe: 11 (4,2,ldg) 12 (4,4,ldg) 13 (2,4,ldg); column
+// indices one step ahead (k_bsr_spmv_pf): 14 (8,2) 15 (8,4) 16 (4,4)
+// 17 (4,2) 18 (8,2,8 CTAs)
+constexpr int kBsrVariants = 19;
 
 template <int MODE, typename T, int LPR>
 static void launch_tma(const Bsr3 &B, const T *val, const T *p, const T *b,
@@ -548,6 +670,17 @@ static void launch_plain(const Bsr3 &B, const T *val, const T *p, const T *b,
     B.nn, B.ptr.p, B.col.p, val, B.pstride, p, b, y, part, flag, dot_out, counter);
 }
 
+template <int MODE, typename T, int L, int U, int M>
+static void launch_pf(const Bsr3 &B, const T *val, const T *p, const T *b, T *y,
+                      double *part, const int *flag, double *dot_out, unsigned *counter,
+                      cudaStream_t st)
+{
+  static int grid = 0;  // per instantiation
+  if(!grid) grid = resident_grid(k_bsr_spmv_pf<MODE, T, L, U, M>, 256, 0);
+  k_bsr_spmv_pf<MODE, T, L, U, M><<<grid, 256, 0, st>>>(
+    B.nn, B.ptr.p, B.col.p, val, B.pstride, p, b, y, part, flag, dot_out, counter);
+}
+
 template <int MODE, typename T>
 static void launch_bsr(int variant, const Bsr3 &B, const T *val, const T *p,
                        const T *b, T *y, double *part, const int *flag,
@@ -570,6 +703,11 @@ static void launch_bsr(int variant, const Bsr3 &B, const T *val, const T *p,
   case 11: GB_BSR(4, 2, 0, 0); break;
   case 12: GB_BSR(4, 4, 0, 0); break;
   case 13: GB_BSR(2, 4, 0, 0); break;
+  case 14: launch_pf<MODE, T, 8, 2, 0>(B, val, p, b, y, part, flag, dot_out, counter, st); break;
+  case 15: launch_pf<MODE, T, 8, 4, 0>(B, val, p, b, y, part, flag, dot_out, counter, st); break;
+  case 16: launch_pf<MODE, T, 4, 4, 0>(B, val, p, b, y, part, flag, dot_out, counter, st); break;
+  case 17: launch_pf<MODE, T, 4, 2, 0>(B, val, p, b, y, part, flag, dot_out, counter, st); break;
+  case 18: launch_pf<MODE, T, 8, 2, 8>(B, val, p, b, y, part, flag, dot_out, counter, st); break;
   default: GB_BSR(8, 2, 1, 0); break;
   }
 #undef GB_BSR
