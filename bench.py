@@ -22,6 +22,7 @@ import argparse
 import ctypes
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -70,7 +71,10 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 comparison solve (profiling runs)")
+    ap.add_argument("--batch-kernel", type=int, default=4,
+                    help="--profile sweep: Batch_Kernel of the batched solve")
     ap.add_argument("--profile", choices=["spmv32", "spmv64", "generate", "step", "twolevel",
+                                          "sweep",
                                           "mpnn"],
                     help="minimal run for ncu: one Generate, then 3 warm-up "
                          "and 3 timed launches of the chosen kernel; 'step': "
@@ -116,6 +120,29 @@ def profile_run(args):
         for _ in range(3):
             net.infer(A)
         print(json.dumps({"profile": "mpnn", "n": n, "nnz": A.nnz()}))
+        return
+    if args.profile == "sweep":
+        # a small batched sweep (64 complex eddy-current problems of 16^2 to
+        # 48^2 cells), solved twice in the one-launch cluster form (FP64
+        # factor, GMRES(40)); the second solve is the one to capture
+        probs = W.eddy_sweep(n_problems=64, seed=7, n_min=16, n_max=48)
+        bt = W.concat_problems(probs)
+        N = bt.dofmap.n_dof
+        terms = G.DeviceTerms(bt.problem, bt.dofmap)
+        A, b, x = LA.gMatrix(N), LA.gVector(N), LA.gVector(N)
+        G.generate(A, b, terms.batch, pattern=True)
+        S = LA.LinAlg_CreateSolver(None)
+        for k, v in dict(Algorithm=8, Preconditioner=6, Krylov_Size=40, Nb_Iter_Max=5000,
+                         Renumbering_Technique=1, Batch_Kernel=args.batch_kernel).items():
+            S.set(k, v)
+        S["stopping_test"] = 1e-10
+        for _ in range(2):
+            infos = LA.LinAlg_SolveBatch(A, b, S, x, bt.offsets)
+        its = [d["iterations"] for d in infos]
+        print(json.dumps({"profile": "sweep", "problems": len(probs), "unknowns": N,
+                          "iterations_min_median_max": [min(its), int(np.median(its)),
+                                                        max(its)],
+                          "one_launch_form": all(d["batch_form"] == 1 for d in infos)}))
         return
     if args.profile == "twolevel":
         # nonlinear 2D magnetostatics at a = 0: one Generate, then two
@@ -325,6 +352,41 @@ def cpu_baseline(n: int, A_csr=None, b=None, iterations=None):
     return total, per_elem, per_iter, sample
 
 
+def host_cpu():
+    """The host CPU's model name and core count (lscpu, else /proc/cpuinfo)."""
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if line.lower().startswith(("model name", "cpu model")):
+                        model = line.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return {"model": model or "unknown", "host_cores": os.cpu_count() or 1,
+            "machine": platform.machine()}
+
+
+def pin_one_core():
+    """Run the single-threaded reference path on one core (as taskset would),
+    so that the measurement does not move between cores; returns the core."""
+    try:
+        core = min(os.sched_getaffinity(0))
+        os.sched_setaffinity(0, {core})
+        return core
+    except (AttributeError, OSError):
+        return None
+
+
 def _rhs_checksum(b):
     b = np.asarray(b, np.float64)
     return float(np.dot(b, np.arange(1, len(b) + 1, dtype=np.float64) % 97.0))
@@ -345,6 +407,8 @@ def run_reference(args, ws, rank):
     import oracle
     from getdp_gb300 import workloads as W
     oracle.build()
+    cpu = host_cpu()
+    cpu["pinned_core"] = pin_one_core()
     n = args.n
     p = W.elasticity_p2(n=n, seed=2)
     dm = W.dofmap_for(p)
@@ -383,6 +447,7 @@ def run_reference(args, ws, rank):
             "full_run": full,
             "sampled_extrapolation_s": float(np.mean(vals)),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                             "cpu": cpu,
                              "sample": json.dumps({"full_run": full,
                                                    "steps_sampled": samples})},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -1201,7 +1266,8 @@ def main():
         total, pe, pi, sample = cpu_baseline(n, (ip, ix, dv), b.numpy(),
                                              info_plain["iterations"])
         line["cpu_baseline"] = {"value": total, "unit": UNIT, "cores": 1,
-                                "kind": "port", "sample": json.dumps(sample),
+                                "kind": "port", "cpu": host_cpu(),
+                                "sample": json.dumps(sample),
                                 "per_element_s": pe, "per_cg_iteration_s": pi}
     if rank == 0:
         print(json.dumps(line))

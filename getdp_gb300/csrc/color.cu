@@ -313,8 +313,14 @@ int colour_build(gb300_matrix *A, int nseg, const int *off)
     for(int v : hc) mx = v > mx ? v : mx;
     C->ncolors = mx + 1;
   }
-  // stable placement, colour by colour, within each block
+  // stable placement, colour by colour, within each block; base[b] counts
+  // the vertices of block b placed so far, so after colour c it closes the
+  // block's colour-c range
   long long placed = 0;
+  const int nc1 = C->ncolors + 1;
+  C->voff.assign((size_t)nseg * nc1, 0);
+  std::vector<long long> hbase(nseg);
+  for(int b = 0; b < nseg; b++) C->voff[(size_t)b * nc1] = vseg[b];
   for(int c = 0; c < C->ncolors; c++) {
     k_colour_flag<<<grid_for(nv, 256), 256, 0, st>>>(nv, color.p, c, flag.p);
     long long cnt = 0;
@@ -325,6 +331,12 @@ int colour_build(gb300_matrix *A, int nseg, const int *off)
                                                        C->old_of.p);
     k_colour_base<<<grid_for(nseg, 256), 256, 0, st>>>(nseg, doff.p, pos.p, base.p);
     placed += cnt;
+    if(cudaMemcpyAsync(hbase.data(), base.p, sizeof(long long) * nseg,
+                       cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+       cudaStreamSynchronize(st) != cudaSuccess)
+      return fail(GB300_ERR_CUDA);
+    for(int b = 0; b < nseg; b++)
+      C->voff[(size_t)b * nc1 + c + 1] = vseg[b] + (int)hbase[b];
   }
   if(placed != nv) return fail(GB300_ERR_UNSUPPORTED);
   // the permuted structure

@@ -45,11 +45,12 @@ namespace gb {
 
 // CTAs per cluster (one cluster per system): Batch_Kernel 1, 2, 4, 8 (the
 // portable maximum) or 16 (a non-portable size this GPU allows).  Measured
-// on 512 complex systems of 1,922..51,842 rows (ILU(0)-GMRES(40), FP64 /
-// FP32 factor): 1 CTA 2.47 / 2.40 s, 2 1.41 / 1.37, 4 1.11 / 1.06, 8 1.31 /
-// 1.26, 16 1.89 / 1.75, against 1.19 / 1.23 s for the per-kernel form: few
-// CTAs leave the largest systems' steps to one or two SMs, many CTAs leave
-// fewer systems running at once and make each cluster barrier dearer
+// on 512 complex systems of 1,922..51,842 rows (ILU(0)-GMRES(40) in the
+// multicolour order, FP64 / FP32 factor): 1 CTA 2.32 / 2.07 s, 2 1.29 /
+// 1.14, 4 0.958 / 0.856, 8 1.11 / 0.99, against 1.19 / 1.235 s for the
+// per-kernel form: few CTAs leave the largest systems' steps to one or two
+// SMs, many CTAs leave fewer systems running at once and make each cluster
+// barrier dearer
 constexpr int kCThreads = 512;
 constexpr int kCWarps = kCThreads / 32;
 constexpr int kCMaxKrylov = 64;
@@ -74,6 +75,11 @@ struct CArgs {
   const int *diag;
   const void *lu, *inv;
   const int *lrows, *urows, *llev, *ulev, *llb, *ulb;
+  // multicolour order: system p's vertices of colour c are
+  // [voff[p (ncol + 1) + c], voff[p (ncol + 1) + c + 1]), bs rows each
+  // (ncol = 0: the level lists above)
+  int ncol, bs;
+  const int *voff;
   double *Vb, *Z, *zt, *u;
   float *t32;
   size_t ldv;
@@ -128,6 +134,25 @@ __device__ __forceinline__ T row_acc(int k0, int k1, const int *__restrict__ col
       }
   }
   return s;
+}
+
+// the sum over the cluster's CTAs and their warps, in (rank, warp) order, of
+// the one partial per warp each CTA left in buf[0 .. kCWarps): every CTA
+// gets the same value in out[0] (no CTA-wide sum first)
+template <int CS>
+__device__ __forceinline__ void cluster_sum_warps(cg::cluster_group &cl, double *buf,
+                                                  double *out)
+{
+  cl.sync();
+  if(threadIdx.x < 32) {
+    double s = 0.;
+    for(int r = 0; r < CS; r++) {
+      double v = threadIdx.x < kCWarps ? cl.map_shared_rank(buf, r)[threadIdx.x] : 0.;
+      s += warp_sum(v);  // lane 0 holds the rank's sum
+    }
+    if(threadIdx.x == 0) out[0] = s;
+  }
+  __syncthreads();
 }
 
 // w = A z on the rows [lo, hi) (two lanes per row, as k_b_spmv); with RES,
@@ -211,6 +236,56 @@ __device__ void c_precond(const CArgs &P, cg::cluster_group &cl, int p, int rank
   }
   const T *lu = (const T *)P.lu, *inv = (const T *)P.inv;
   cl.sync();  // src written by every CTA
+  if(P.ncol > 0) {
+    // colour by colour: a colour's vertices share no entry, so they are
+    // independent; a vertex's bs rows (a complex unknown's two real rows)
+    // go in order in one thread, forward first to last, backward last to
+    // first: one barrier per colour instead of one per level
+    const int *vo = P.voff + (size_t)p * (P.ncol + 1);
+    const int bs = P.bs;
+    for(int c = 0; c < P.ncol; c++) {
+      const int a = vo[c], cnt = vo[c + 1] - a;
+      if(cnt == 0) continue;  // the same for every CTA
+      const int t0 = a + (int)((long long)cnt * rank / CS);
+      const int t1 = a + (int)((long long)cnt * (rank + 1) / CS);
+      for(int v = t0 + threadIdx.x; v < t1; v += kCThreads)
+        for(int q = 0; q < bs; q++) {
+          const int i = v * bs + q;
+          if constexpr(sizeof(T) == 8)
+            dst[i] = row_acc<1, true>(P.rowptr[i], P.diag[i], P.col, lu,
+                                      (const double *)dst, __ldcg(src + i));
+          else
+            P.t32[i] = row_acc<1, true>(P.rowptr[i], P.diag[i], P.col, lu,
+                                        (const float *)P.t32, (float)__ldcg(src + i));
+        }
+      cl.sync();
+    }
+    for(int c = P.ncol - 1; c >= 0; c--) {
+      const int a = vo[c], cnt = vo[c + 1] - a;
+      if(cnt == 0) continue;
+      const int t0 = a + (int)((long long)cnt * rank / CS);
+      const int t1 = a + (int)((long long)cnt * (rank + 1) / CS);
+      for(int v = t0 + threadIdx.x; v < t1; v += kCThreads)
+        for(int q = bs - 1; q >= 0; q--) {
+          const int i = v * bs + q;
+          const int ke = P.rowptr[i + 1];
+          if constexpr(sizeof(T) == 8) {
+            double s = row_acc<1, true>(P.diag[i] + 1, ke, P.col, lu, (const double *)dst,
+                                        __ldcg(dst + i));
+            dst[i] = inv[i] * s;
+          }
+          else {
+            float s = row_acc<1, true>(P.diag[i] + 1, ke, P.col, lu, (const float *)P.t32,
+                                       __ldcg(P.t32 + i));
+            float w = inv[i] * s;
+            P.t32[i] = w;
+            dst[i] = (double)w;
+          }
+        }
+      cl.sync();
+    }
+    return;
+  }
   for(int l = P.llb[p]; l + 1 < P.llb[p + 1]; l++) {
     const int a = P.llev[l], cnt = P.llev[l + 1] - a;
     const int t0 = a + (int)((long long)cnt * rank / CS);
@@ -288,10 +363,9 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
       // restart: r = b - A x into V_0, ||r||
       cl.sync();  // x complete
       {
-        double rr = c_spmv<1>(P, lo, hi, P.x, P.Vb, nullptr);
-        rr = block_sum<double, kCThreads>(rr);
-        if(tid == 0) xbuf[xb][0] = rr;
-        cluster_sum<CS>(cl, xbuf[xb], 1, sdot);
+        double rr = warp_sum(c_spmv<1>(P, lo, hi, P.x, P.Vb, nullptr));
+        if((tid & 31) == 0) xbuf[xb][tid >> 5] = rr;
+        cluster_sum_warps<CS>(cl, xbuf[xb], sdot);
         xb ^= 1;
       }
       if(tid == 0) {
@@ -343,19 +417,17 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
             S.cycle = 0;
             S.reorth = 0;
           }
-          else
-            for(int j = 0; j < k; j++) {
-              sh1[j] = sdot[j];
-              sH[(k - 1) * (m + 1) + j] = sdot[j];
-            }
+        }
+        if(tid < k) {
+          sh1[tid] = sdot[tid];
+          sH[(k - 1) * (m + 1) + tid] = sdot[tid];
         }
         __syncthreads();
         if(!S.cycle) break;
         {
-          double v = c_update(P, lo, hi, w, sh1, k);
-          v = block_sum<double, kCThreads>(v);
-          if(tid == 0) xbuf[xb][0] = v;
-          cluster_sum<CS>(cl, xbuf[xb], 1, sdot);
+          double v = warp_sum(c_update(P, lo, hi, w, sh1, k));
+          if((tid & 31) == 0) xbuf[xb][tid >> 5] = v;
+          cluster_sum_warps<CS>(cl, xbuf[xb], sdot);
           xb ^= 1;
         }
         if(tid == 0) {
@@ -368,13 +440,11 @@ __global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
           c_dots(P, lo, hi, w, k, xbuf[xb]);
           cluster_sum<CS>(cl, xbuf[xb], k, sdot);
           xb ^= 1;
-          if(tid == 0)
-            for(int j = 0; j < k; j++) sH[(k - 1) * (m + 1) + j] = sh1[j] + sdot[j];
+          if(tid < k) sH[(k - 1) * (m + 1) + tid] = sh1[tid] + sdot[tid];
           __syncthreads();
-          double v = c_update(P, lo, hi, w, sdot, k);
-          v = block_sum<double, kCThreads>(v);
-          if(tid == 0) xbuf[xb][0] = v;
-          cluster_sum<CS>(cl, xbuf[xb], 1, sdot);
+          double v = warp_sum(c_update(P, lo, hi, w, sdot, k));
+          if((tid & 31) == 0) xbuf[xb][tid >> 5] = v;
+          cluster_sum_warps<CS>(cl, xbuf[xb], sdot);
           xb ^= 1;
           if(tid == 0) S.rr = sdot[0];
           __syncthreads();
@@ -556,7 +626,7 @@ static int launch_c(const CArgs &a, cudaStream_t st, int *nclusters)
 int gmres_solve_batch_cluster(gb300_matrix *A, const double *val, const double *rhs,
                               double *x, const gb300_solver_params *p, int nsys,
                               const int *off, gb300_solve_info *infos, Work &W,
-                              bool *used)
+                              bool *used, const Colouring *mc)
 {
   *used = false;
   const int cs = p->batch_kernel;
@@ -579,9 +649,24 @@ int gmres_solve_batch_cluster(gb300_matrix *A, const double *val, const double *
   const bool precond = (p->preconditioner == 6);
   const bool fp32 = (p->precision != 0);
   const SysLevels *SL = nullptr;
+  // the multicolour order's colour ranges, when A is its permuted copy and
+  // they describe the same systems; else the level lists of the schedule
+  const bool by_colour = precond && mc && mc->B == A &&
+                         (int)mc->seg.size() == nsys + 1 &&
+                         std::equal(off, off + nsys + 1, mc->seg.begin()) &&
+                         (int)mc->voff.size() == nsys * (mc->ncolors + 1);
+  DevBuf<int> dvoff;
   if(precond) {
-    GB_TRY(ilu_sys_levels(A, nsys, off, &SL));
-    if(SL->max_levels > kCMaxLevels) return GB300_OK;
+    if(by_colour) {
+      if(mc->ncolors > kCMaxLevels) return GB300_OK;
+      GB_TRY(dvoff.alloc(mc->voff.size()));
+      GB_CUDA(cudaMemcpyAsync(dvoff.p, mc->voff.data(), sizeof(int) * mc->voff.size(),
+                              cudaMemcpyHostToDevice, st));
+    }
+    else {
+      GB_TRY(ilu_sys_levels(A, nsys, off, &SL));
+      if(SL->max_levels > kCMaxLevels) return GB300_OK;
+    }
     int zr = 0;
     GB_TRY(ilu_factor(A, val, fp32, &zr));
     if(zr) {
@@ -633,12 +718,19 @@ int gmres_solve_batch_cluster(gb300_matrix *A, const double *val, const double *
   a.x = x;
   if(precond) {
     ilu_factor_arrays(A, fp32, &a.lu, &a.inv, &a.diag);
-    a.lrows = SL->lrows.p;
-    a.urows = SL->urows.p;
-    a.llev = SL->llev.p;
-    a.ulev = SL->ulev.p;
-    a.llb = SL->llb.p;
-    a.ulb = SL->ulb.p;
+    if(by_colour) {
+      a.ncol = mc->ncolors;
+      a.bs = mc->bs;
+      a.voff = dvoff.p;
+    }
+    else {
+      a.lrows = SL->lrows.p;
+      a.urows = SL->urows.p;
+      a.llev = SL->llev.p;
+      a.ulev = SL->ulev.p;
+      a.llb = SL->llb.p;
+      a.ulb = SL->ulb.p;
+    }
   }
   a.Vb = Vb;
   a.Z = Z;

@@ -1029,7 +1029,8 @@ int solve_batch(gb300_matrix *A, const gb300_vector *bvec,
     GB_TRY(yb.alloc(n));
     permute_system(C, A->nnz, val, rhs, B->val.p, rb.p, st);
     bool used = false;
-    GB_TRY(gmres_solve_batch_cluster(B, B->val.p, rb.p, yb.p, p, nsys, off, infos, W, &used));
+    GB_TRY(gmres_solve_batch_cluster(B, B->val.p, rb.p, yb.p, p, nsys, off, infos, W, &used,
+                                     C));
     if(!used) GB_TRY(gmres_solve_batch(B, B->val.p, rb.p, yb.p, p, nsys, off, infos, W));
     unpermute_solution(C, yb.p, x, st);
   }

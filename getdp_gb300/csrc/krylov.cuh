@@ -210,10 +210,13 @@ void ilu_factor_arrays(const gb300_matrix *A, bool fp32, const void **lu, const 
 // batched GMRES/FGMRES with one thread-block cluster per system and the
 // whole solve in one launch (gmres_cluster.cu); *used is false, and nothing
 // is done, where that form does not apply (then gmres_solve_batch does)
+// mc: the multicolour ordering A is permuted by (A = mc->B), or null: with
+// it the ILU(0) sweeps go colour by colour, a vertex's rows in one thread
+struct Colouring;
 int gmres_solve_batch_cluster(gb300_matrix *A, const double *val, const double *rhs,
                               double *x, const gb300_solver_params *p, int nsys,
                               const int *off, gb300_solve_info *infos, Work &W,
-                              bool *used);
+                              bool *used, const Colouring *mc = nullptr);
 int check_blocks(const gb300_matrix *A, int nsys, const int *off);
 
 // multicolour ordering of a pattern for the ILU(0) solves (color.cu)
@@ -222,6 +225,9 @@ struct Colouring {
   unsigned version = 0;        // pattern version it was built for
   std::vector<int> seg;        // diagonal blocks it was built for
   int bs = 1;                  // rows per coloured vertex
+  // per block b, the vertices of colour c are [voff[b (ncolors + 1) + c],
+  // voff[b (ncolors + 1) + c + 1]) in the permuted order
+  std::vector<int> voff;
   DevBuf<int> new_of, old_of;  // row permutation and its inverse
   DevBuf<int> src;             // entry k of the permuted matrix = entry src[k] of A
   gb300_matrix *B = nullptr;   // permuted structure (+ its ILU state)
