@@ -249,20 +249,51 @@ k_mp_layer_mma(int n, const int *__restrict__ rowptr, const int *__restrict__ co
   }
   const int ntiles = (n + 15) / 16;
   for(int t = blockIdx.x * kMmaWarps + warp; t < ntiles; t += gridDim.x * kMmaWarps) {
-    // messages of the tile's 16 nodes, lane = channel
-    for(int r = 0; r < 16; r++) {
+    // messages of the tile's 16 nodes: lane = (node r, half hf of the
+    // channels), each neighbour's 16 channels gathered as four float4, so a
+    // warp walks its 16 rows side by side (each channel summed in the row's
+    // order, as in k_mp_layer)
+    {
+      const int r = lane >> 1, hf = lane & 1;
       const int i = 16 * t + r;
-      float hi = 0.f, mi = 0.f;
+      float4 mi[4], hv[4];
+#pragma unroll
+      for(int q = 0; q < 4; q++) mi[q] = hv[q] = make_float4(0.f, 0.f, 0.f, 0.f);
       if(i < n) {
         for(int k = rowptr[i]; k < rowptr[i + 1]; k++) {
           const int j = col[k];
-          if(j != i) mi += ehat[k] * hin[(size_t)j * kH + lane];
+          if(j == i) continue;
+          const float e = ehat[k];
+          const float4 *hj = reinterpret_cast<const float4 *>(hin + (size_t)j * kH + 16 * hf);
+#pragma unroll
+          for(int q = 0; q < 4; q++) {
+            const float4 v = __ldg(hj + q);
+            mi[q].x += e * v.x;
+            mi[q].y += e * v.y;
+            mi[q].z += e * v.z;
+            mi[q].w += e * v.w;
+          }
         }
-        hi = hin[(size_t)i * kH + lane];
-        mout[(size_t)i * kH + lane] = mi;
+        const float4 *hs = reinterpret_cast<const float4 *>(hin + (size_t)i * kH + 16 * hf);
+        float4 *mo = reinterpret_cast<float4 *>(mout + (size_t)i * kH + 16 * hf);
+#pragma unroll
+        for(int q = 0; q < 4; q++) {
+          hv[q] = __ldg(hs + q);
+          mo[q] = mi[q];
+        }
       }
-      X[warp][r][lane] = hi;
-      X[warp][r][kH + lane] = mi;
+#pragma unroll
+      for(int q = 0; q < 4; q++) {
+        const int c = 16 * hf + 4 * q;
+        X[warp][r][c] = hv[q].x;
+        X[warp][r][c + 1] = hv[q].y;
+        X[warp][r][c + 2] = hv[q].z;
+        X[warp][r][c + 3] = hv[q].w;
+        X[warp][r][kH + c] = mi[q].x;
+        X[warp][r][kH + c + 1] = mi[q].y;
+        X[warp][r][kH + c + 2] = mi[q].z;
+        X[warp][r][kH + c + 3] = mi[q].w;
+      }
     }
     __syncwarp();
     float C[4][4];
