@@ -50,7 +50,9 @@ namespace gb {
 // 1.14, 4 0.958 / 0.856, 8 1.11 / 0.99, against 1.19 / 1.235 s for the
 // per-kernel form: few CTAs leave the largest systems' steps to one or two
 // SMs, many CTAs leave fewer systems running at once and make each cluster
-// barrier dearer
+// barrier dearer.  256-thread CTAs measured the same at the same threads
+// per system (8 CTAs: 0.938 / 0.843 s) and slower at fewer (4 CTAs: 1.22 /
+// 1.10 s)
 constexpr int kCThreads = 512;
 constexpr int kCWarps = kCThreads / 32;
 constexpr int kCMaxKrylov = 64;
@@ -327,7 +329,7 @@ __device__ void c_precond(const CArgs &P, cg::cluster_group &cl, int p, int rank
 }
 
 template <typename T, int CS>
-__global__ void __launch_bounds__(kCThreads, 2) k_c_solve(CArgs P)
+__global__ void __launch_bounds__(kCThreads, 1024 / kCThreads) k_c_solve(CArgs P)
 {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
