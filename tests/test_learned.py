@@ -274,8 +274,14 @@ def test_gpu_two_level_correction_reduces_steps_on_held_out_systems():
     at 256^2) on held-out systems of the same distribution (seeds 5, 6):
     FGMRES with it (Preconditioner 22) takes fewer steps than the cycle
     without it (21) and reaches the same solution.  It does not take less
-    time: the correction costs two more sparse products per smoothing."""
+    time than 21: the correction costs two more sparse products per
+    smoothing.  Against plain ILU(0)-FGMRES (Preconditioner 6) the learned
+    arm takes far fewer steps and less wall time -- a gain of the coarse
+    level of the cycle, which the correction is trained inside, more than
+    of the network.  Each solver is timed on its second solve (the first
+    makes the colouring, the factor's schedule and the CUDA graphs)."""
     import os
+    import time
     G, LR, LA = _gpu()
     wfile = os.path.join(os.path.dirname(LR.__file__), "weights",
                          "mpnn_nl2d_256_twolevel.npy")
@@ -290,18 +296,27 @@ def test_gpu_two_level_correction_reduces_steps_on_held_out_systems():
         agg, nc = W.cell_aggregates(p, dm, 8)
         A.set_aggregates(agg, nc)
         net.infer(A)
-        sols, steps = [], []
-        for prec in (21, 22):
+        sols, steps, secs = [], [], []
+        for prec in (21, 22, 6):
             S = LA.LinAlg_CreateSolver(None)
             for k, v in dict(Algorithm=9, Preconditioner=prec, Krylov_Size=50,
-                             Nb_Iter_Max=2000, Renumbering_Technique=1, Precision=1).items():
+                             Nb_Iter_Max=20000, Renumbering_Technique=1,
+                             Precision=1).items():
                 S.set(k, v)
             S["stopping_test"] = 1e-10
             x = LA.gVector(dm.n_dof)
-            info = LA.LinAlg_Solve(A, b, S, x)
+            for _ in range(2):
+                t0 = time.perf_counter()
+                info = LA.LinAlg_Solve(A, b, S, x)
+                dt = time.perf_counter() - t0
             assert info["status"] == 0
             sols.append(x.numpy())
             steps.append(info["iterations"])
-        print(f"seed {seed}: two-level {steps[0]} steps, with the correction {steps[1]}")
+            secs.append(dt)
+        print(f"seed {seed}: two-level {steps[0]} steps {secs[0]:.4f} s, with the "
+              f"correction {steps[1]} steps {secs[1]:.4f} s, ILU(0) {steps[2]} steps "
+              f"{secs[2]:.4f} s")
         assert steps[1] <= 0.95 * steps[0]
         assert np.linalg.norm(sols[1] - sols[0]) <= 1e-6 * np.linalg.norm(sols[0])
+        assert steps[1] < steps[2] and secs[1] < secs[2]
+        assert np.linalg.norm(sols[2] - sols[1]) <= 1e-6 * np.linalg.norm(sols[2])
