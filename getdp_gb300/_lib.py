@@ -145,6 +145,7 @@ SIGNATURES = {
     "gb300_mpnn_set_loss": (_I, [_P, _I]),
     "gb300_post_elements": (_I, [ctypes.POINTER(TermBatch), _P, _P]),
     "gb300_post_points": (_I, [ctypes.POINTER(TermBatch), _P, _I, _P, _P, _P, _P]),
+    "gb300_rcmk_order": (_I, [_I, _P, _P, _P]),
     "gb300_solve_batch": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, _I,
                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(SolveInfo)]),
     "gb300_event_record": (_I, [_P, _I]),

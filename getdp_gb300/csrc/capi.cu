@@ -974,6 +974,30 @@ int gb300_post_points(const gb300_term_batch *t, const gb300_vector *x, int npts
   return post_points(t, x, npts, xyz, field, curl, elem);
 }
 
+int gb300_rcmk_order(int n, const int *rowptr, const int *col, int *new_of)
+{
+  GB_TRY(check(rowptr, "rowptr"));
+  GB_TRY(check(col, "col"));
+  GB_TRY(check(new_of, "new_of"));
+  if(n < 0 || rowptr[0] != 0) {
+    set_error("gb300_rcmk_order: bad pattern");
+    return GB300_ERR_ARG;
+  }
+  for(int i = 0; i < n; i++) {
+    if(rowptr[i + 1] < rowptr[i]) {
+      set_error("gb300_rcmk_order: row pointers decrease at row %d", i);
+      return GB300_ERR_ARG;
+    }
+    for(int k = rowptr[i]; k < rowptr[i + 1]; k++)
+      if(col[k] < 0 || col[k] >= n) {
+        set_error("gb300_rcmk_order: column %d out of range in row %d", col[k], i);
+        return GB300_ERR_ARG;
+      }
+  }
+  gb::rcmk_order(n, rowptr, col, new_of);
+  return GB300_OK;
+}
+
 int gb300_solve_batch(gb300_matrix *A, const gb300_vector *b,
                       const gb300_solver_params *p, gb300_vector *x, int nsys,
                       const int *offsets, gb300_solve_info *infos)

@@ -241,6 +241,8 @@ void colour_free(Colouring *c)
 // A->block_rows rows, and the permuted matrix structure;
 // GB300_ERR_UNSUPPORTED when the pattern does not allow it (the caller then
 // keeps GetDP's order)
+static int permuted_structure(gb300_matrix *A, Colouring *C, cudaStream_t st);
+
 int colour_build(gb300_matrix *A, int nseg, const int *off)
 {
   const int n = A->n;
@@ -249,7 +251,7 @@ int colour_build(gb300_matrix *A, int nseg, const int *off)
   for(int v : seg)
     if(v % bs) bs = 1;
   if(n % bs) bs = 1;
-  if(A->mc && A->mc->version == A->pattern_version && A->mc->n == n &&
+  if(A->mc && A->mc->kind == 0 && A->mc->version == A->pattern_version && A->mc->n == n &&
      A->mc->seg == seg && A->mc->bs == bs)
     return GB300_OK;
   colour_free(A->mc);
@@ -339,31 +341,150 @@ int colour_build(gb300_matrix *A, int nseg, const int *off)
       C->voff[(size_t)b * nc1 + c + 1] = vseg[b] + (int)hbase[b];
   }
   if(placed != nv) return fail(GB300_ERR_UNSUPPORTED);
-  // the permuted structure
+  const int rc_ = permuted_structure(A, C, st);
+  if(rc_ != GB300_OK) return fail(rc_);
+  A->mc = C;
+  return GB300_OK;
+}
+
+// B = P A P^T for the row permutation C->new_of / C->old_of (rows sorted by
+// the new column index, as Sparskit's sortcol leaves them), with C->src the
+// position in A of each of B's entries; GB300_ERR_UNSUPPORTED when a row is
+// longer than the sort's capacity
+static int permuted_structure(gb300_matrix *A, Colouring *C, cudaStream_t st)
+{
+  const int n = A->n;
+  DevBuf<int> len, err;
+  DevBuf<long long> brp, tmp;
   gb300_matrix *B = new gb300_matrix();
   C->B = B;
   B->ctx = A->ctx;
   B->n = n;
   B->nnz = A->nnz;
-  if(len.alloc(n + 1) || brp.alloc(n + 1) || B->rowptr.alloc(n + 1) ||
-     B->col.alloc(A->nnz > 0 ? A->nnz : 1) || B->val.alloc(A->nnz > 0 ? A->nnz : 1) ||
-     C->src.alloc(A->nnz > 0 ? A->nnz : 1))
-    return fail(GB300_ERR_CUDA);
+  GB_TRY(len.alloc(n + 1));
+  GB_TRY(err.alloc(1));
+  GB_TRY(brp.alloc(n + 1));
+  GB_TRY(B->rowptr.alloc(n + 1));
+  GB_TRY(B->col.alloc(A->nnz > 0 ? A->nnz : 1));
+  GB_TRY(B->val.alloc(A->nnz > 0 ? A->nnz : 1));
+  GB_TRY(C->src.alloc(A->nnz > 0 ? A->nnz : 1));
   k_perm_len<<<grid_for(n + 1, 256), 256, 0, st>>>(n, A->rowptr.p, C->old_of.p, len.p);
   long long total = 0;
-  int rc = exclusive_scan(len.p, n + 1, brp.p, &total, tmp, st);
-  if(rc != GB300_OK) return fail(rc);
-  if(total != A->nnz) return fail(GB300_ERR_UNSUPPORTED);
+  GB_TRY(exclusive_scan(len.p, n + 1, brp.p, &total, tmp, st));
+  if(total != A->nnz) return GB300_ERR_UNSUPPORTED;
   k_i64_to_i32_rows<<<grid_for(n + 1, 256), 256, 0, st>>>(brp.p, n + 1, B->rowptr.p);
-  if(cudaMemsetAsync(err.p, 0, sizeof(int), st) != cudaSuccess) return fail(GB300_ERR_CUDA);
+  GB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
   k_perm_rows<<<grid_for(n, kPermWarps), 32 * kPermWarps, 0, st>>>(
     n, A->rowptr.p, A->col.p, C->new_of.p, C->old_of.p, brp.p, B->col.p, C->src.p, err.p);
-  if(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-     cudaStreamSynchronize(st) != cudaSuccess)
-    return fail(GB300_ERR_CUDA);
-  if(herr) return fail(GB300_ERR_UNSUPPORTED);
+  int herr = 0;
+  GB_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if(herr) return GB300_ERR_UNSUPPORTED;
   B->csr_valid = true;
   choose_tpr(B);
+  return GB300_OK;
+}
+
+// The reverse Cuthill-McKee order of Sparskit's cmkreord (cmkreord.f:3-30,
+// with perphn, BFS, add_lvst and rversp of reordering.f:15-380), as
+// Renumbering_Technique 1 runs it before the ILU (Sparskit.cpp:245-256):
+// a breadth-first search from row 0 lists the rows level by level (a row's
+// unlisted neighbours appended in the order its CSR row holds them; when a
+// connected component is exhausted, the next unlisted row by index starts
+// the next level); while the search from a row of the last level with the
+// fewest entries (the first such row) yields more levels, it is repeated
+// from there (a pseudo-peripheral start); the listing of the last search,
+// reversed, is the new order.  new_of[i] is the new index of row i.
+void rcmk_order(int n, const int *rowptr, const int *col, int *new_of)
+{
+  if(n <= 0) return;
+  std::vector<int> order(n), lev;
+  std::vector<char> seen(n);
+  auto search = [&](int start) {
+    std::fill(seen.begin(), seen.end(), 0);
+    lev.clear();
+    int head = 0, tail = 0, next = 0;
+    order[tail++] = start;
+    seen[start] = 1;
+    for(;;) {
+      lev.push_back(head);
+      const int end = tail;
+      for(int t = head; t < end; t++) {
+        const int i = order[t];
+        for(int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+          const int j = col[k];
+          if(!seen[j]) {
+            seen[j] = 1;
+            order[tail++] = j;
+          }
+        }
+      }
+      head = end;
+      if(head < tail) continue;
+      while(next < n && seen[next]) next++;
+      if(next >= n) break;
+      seen[next] = 1;
+      order[tail++] = next;
+    }
+    lev.push_back(tail);
+    return (int)lev.size() - 1;  // levels
+  };
+  int start = 0, best = 0;
+  for(;;) {
+    const int nl = search(start);
+    if(nl <= best) break;
+    best = nl;
+    // the first row of the last level with the fewest entries (fewer than
+    // the number of rows listed)
+    int mindeg = lev[nl];
+    for(int t = lev[nl - 1]; t < lev[nl]; t++) {
+      const int i = order[t], deg = rowptr[i + 1] - rowptr[i];
+      if(deg < mindeg) {
+        start = i;
+        mindeg = deg;
+      }
+    }
+  }
+  for(int t = 0; t < n; t++) new_of[order[n - 1 - t]] = t;
+}
+
+// The RCMK order of A's pattern (Renumbering_Technique 2 of this backend:
+// the reference's Renumbering_Technique 1) and the permuted structure,
+// cached with A's pattern version like the multicolour ordering
+int rcmk_build(gb300_matrix *A)
+{
+  const int n = A->n;
+  if(A->mc && A->mc->kind == 1 && A->mc->version == A->pattern_version && A->mc->n == n)
+    return GB300_OK;
+  colour_free(A->mc);
+  A->mc = nullptr;
+  cudaStream_t st = A->ctx->stream;
+  std::vector<int> rp(n + 1), ci(A->nnz > 0 ? A->nnz : 1), no(n), oo(n);
+  GB_CUDA(cudaMemcpyAsync(rp.data(), A->rowptr.p, sizeof(int) * (n + 1),
+                          cudaMemcpyDeviceToHost, st));
+  if(A->nnz > 0)
+    GB_CUDA(cudaMemcpyAsync(ci.data(), A->col.p, sizeof(int) * A->nnz,
+                            cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  rcmk_order(n, rp.data(), ci.data(), no.data());
+  for(int i = 0; i < n; i++) oo[no[i]] = i;
+  Colouring *C = new Colouring();
+  C->n = n;
+  C->version = A->pattern_version;
+  C->kind = 1;
+  int rc = C->new_of.alloc(n);
+  if(rc == GB300_OK) rc = C->old_of.alloc(n);
+  if(rc == GB300_OK &&
+     (cudaMemcpyAsync(C->new_of.p, no.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st) !=
+        cudaSuccess ||
+      cudaMemcpyAsync(C->old_of.p, oo.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st) !=
+        cudaSuccess))
+    rc = GB300_ERR_CUDA;
+  if(rc == GB300_OK) rc = permuted_structure(A, C, st);
+  if(rc != GB300_OK) {
+    colour_free(C);
+    return rc;
+  }
   A->mc = C;
   return GB300_OK;
 }
@@ -388,7 +509,7 @@ int gmres_solve_coloured(gb300_matrix *A, const double *val, const double *rhs,
 {
   *used = false;
   const int whole[2] = {0, A->n};
-  int rc = colour_build(A, 1, whole);
+  int rc = p->renumbering_technique == 2 ? rcmk_build(A) : colour_build(A, 1, whole);
   if(rc == GB300_ERR_UNSUPPORTED) return GB300_OK;
   if(rc != GB300_OK) return rc;
   *used = true;
@@ -454,9 +575,9 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
   const double *vin = v;
   double *zout = z;
   Colouring *C = nullptr;
-  if(p->renumbering_technique == 1 && !sai) {
+  if((p->renumbering_technique == 1 || p->renumbering_technique == 2) && !sai) {
     const int whole[2] = {0, n};
-    int rc = colour_build(A, 1, whole);
+    int rc = p->renumbering_technique == 2 ? rcmk_build(A) : colour_build(A, 1, whole);
     if(rc != GB300_OK && rc != GB300_ERR_UNSUPPORTED) return rc;
     if(rc == GB300_OK) {
       C = A->mc;

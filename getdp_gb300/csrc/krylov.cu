@@ -903,7 +903,9 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
     // Renumbering_Technique 1 (RCMK in Sparskit): this backend's own
     // renumbering, a multicolour ordering, for the ILU(0) solves
     bool used = false;
-    if(p->renumbering_technique == 1 &&
+    // Renumbering_Technique 2 (no Sparskit value): the reference's RCMK
+    // order itself, for its default iteration trajectory
+    if((p->renumbering_technique == 1 || p->renumbering_technique == 2) &&
        (p->preconditioner == 6 || p->preconditioner == kPrecondLearned ||
         p->preconditioner == kPrecondCoarse || p->preconditioner == kPrecondLearnedCoarse ||
         p->preconditioner == kPrecondLearnedCoarsePre)) {

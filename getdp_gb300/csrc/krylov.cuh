@@ -221,6 +221,7 @@ int check_blocks(const gb300_matrix *A, int nsys, const int *off);
 
 // multicolour ordering of a pattern for the ILU(0) solves (color.cu)
 struct Colouring {
+  int kind = 0;  // 0 multicolour ordering, 1 the RCMK order (rcmk_build)
   int n = 0, ncolors = 0;
   unsigned version = 0;        // pattern version it was built for
   std::vector<int> seg;        // diagonal blocks it was built for
@@ -234,6 +235,9 @@ struct Colouring {
 };
 void colour_free(Colouring *c);
 int colour_build(gb300_matrix *A, int nseg, const int *off);
+// Sparskit's reverse Cuthill-McKee order (host) and A permuted by it
+void rcmk_order(int n, const int *rowptr, const int *col, int *new_of);
+int rcmk_build(gb300_matrix *A);
 void permute_system(const Colouring *C, long long nnz, const double *val,
                     const double *rhs, double *bval, double *brhs, cudaStream_t st);
 void unpermute_solution(const Colouring *C, const double *y, double *x, cudaStream_t st);

@@ -68,7 +68,11 @@ typedef struct gb300_solver_params {
   int matrix_printing;
   int matrix_storage;
   int scaling;
-  int renumbering_technique;
+  int renumbering_technique; /* 1 (Sparskit's RCMK): this backend's multicolour
+                                order for the ILU(0) sweeps; 2 (no Sparskit
+                                value): the reference's RCMK order itself
+                                (its default iteration trajectory, serial
+                                level schedule); 0 GetDP's order */
   int preconditioner;
   int preconditioner_position;
   int nb_fill;
@@ -416,6 +420,13 @@ int gb300_mpnn_set_loss(gb300_mpnn *net, int mode);
 int gb300_solve(gb300_matrix *A, const gb300_vector *b,
                 const gb300_solver_params *p, gb300_vector *x,
                 gb300_solve_info *info);
+
+/* The reverse Cuthill-McKee order Sparskit computes for Renumbering_Technique
+   1 (cmkreord, contrib/Sparskit/cmkreord.f:3-30, called at
+   Sparskit.cpp:247-250): new_of[i] is the new index of row i of the n x n
+   pattern (0-based CSR, host arrays; structurally symmetric patterns as the
+   ILU needs).  Host only; gb300_solve uses it for Renumbering_Technique 2. */
+int gb300_rcmk_order(int n, const int *rowptr, const int *col, int *new_of);
 
 /* Batched LinAlg_Solve (Sparskit.cpp:108-634 once per system): the nsys
    independent systems are the diagonal blocks of A, system k owning rows

@@ -279,3 +279,34 @@ def newton(problem, dofmap, tol=1e-8, iter_max=50, relaxation=(1.0,), **solve_kw
         hist.append(res)
     return x, np.array(hist), its
 
+
+def rcmk_new_of(indptr, indices):
+    """The reference's RCMK permutation (the restated cmkreord, as
+    Sparskit.cpp:247-250 calls it) of a 0-based CSR pattern: new_of[i] is the
+    new 0-based index of row i."""
+    L = lib()
+    n = len(indptr) - 1
+    nnz = int(indptr[-1])
+    ia = np.ascontiguousarray(np.asarray(indptr) + 1, np.int32)
+    ja = np.ascontiguousarray(np.asarray(indices) + 1, np.int32)
+    a = np.zeros(max(nnz, 1), np.float64)
+    a0 = np.zeros(max(nnz, 1), np.float64)
+    ja0 = np.zeros(max(nnz, 1), np.int32)
+    ia0 = np.zeros(n + 1, np.int32)
+    iperm = np.zeros(n, np.int32)
+    mask = np.zeros(max(nnz, n), np.int32)
+    riord = np.zeros(n, np.int32)
+    levels = np.zeros(n + 1, np.int32)
+    init, maskval, nlev = ctypes.c_int(1), ctypes.c_int(1), ctypes.c_int(1)
+    P = ctypes.POINTER
+    f = L.cmkreord_
+    f.restype = None
+    f(ctypes.byref(ctypes.c_int(n)), a.ctypes.data_as(P(ctypes.c_double)),
+      ja.ctypes.data_as(P(ctypes.c_int)), ia.ctypes.data_as(P(ctypes.c_int)),
+      a0.ctypes.data_as(P(ctypes.c_double)), ja0.ctypes.data_as(P(ctypes.c_int)),
+      ia0.ctypes.data_as(P(ctypes.c_int)), ctypes.byref(init),
+      iperm.ctypes.data_as(P(ctypes.c_int)), mask.ctypes.data_as(P(ctypes.c_int)),
+      ctypes.byref(maskval), ctypes.byref(nlev), riord.ctypes.data_as(P(ctypes.c_int)),
+      levels.ctypes.data_as(P(ctypes.c_int)))
+    return iperm - 1
+
