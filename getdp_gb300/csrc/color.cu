@@ -608,7 +608,7 @@ int precond_apply(gb300_matrix *A, const gb300_solver_params *p, const double *v
       spmv_guarded(M, M->corr.p, vv, zz, nullptr, st);
       return;
     }
-    ilu_apply(M, fp32, vv, zz, fp32 ? t32.p : nullptr, nullptr, st);
+    ilu_apply(M, ilu_mode(p), vv, zz, fp32 ? t32.p : nullptr, nullptr, st);
     if(corr) correction_apply(M, M->val.p, vv, zz, t1.p, t2.p, nullptr, st);
   };
   if(p->preconditioner == kPrecondSai) GB_TRY(spai1(M, M->val.p));

@@ -369,37 +369,38 @@ __device__ __forceinline__ void row_fact(int i, const int *__restrict__ rowptr,
     inv[i] = (T)(1.0 / (double)piv);
 }
 
-template <typename T>
+// T: the factor's storage type; X: the vectors' (and the arithmetic's) type
+template <typename T, typename X = T>
 __device__ __forceinline__ void row_fwd(int i, const int *__restrict__ rowptr,
                                         const int *__restrict__ col,
                                         const int *__restrict__ diag,
-                                        const T *__restrict__ lu, const T *src, T *x)
+                                        const T *__restrict__ lu, const X *src, X *x)
 {
-  T s = src[i];  // the right-hand side's entry (src may be x itself)
-  for(int k = rowptr[i]; k < diag[i]; k++) s = s - lu[k] * x[col[k]];
+  X s = src[i];  // the right-hand side's entry (src may be x itself)
+  for(int k = rowptr[i]; k < diag[i]; k++) s = s - (X)lu[k] * x[col[k]];
   x[i] = s;
 }
 
-template <typename T>
+template <typename T, typename X = T>
 __device__ __forceinline__ void row_bwd(int i, const int *__restrict__ rowptr,
                                         const int *__restrict__ col,
                                         const int *__restrict__ diag,
                                         const T *__restrict__ lu,
-                                        const T *__restrict__ inv, T *x)
+                                        const T *__restrict__ inv, X *x)
 {
-  T s = x[i];
-  for(int k = diag[i] + 1; k < rowptr[i + 1]; k++) s = s - lu[k] * x[col[k]];
-  x[i] = inv[i] * s;
+  X s = x[i];
+  for(int k = diag[i] + 1; k < rowptr[i + 1]; k++) s = s - (X)lu[k] * x[col[k]];
+  x[i] = (X)inv[i] * s;
 }
 
 // MODE 0 factor, 1 forward solve, 2 backward solve
-template <int MODE, typename T>
+template <int MODE, typename T, typename X = T>
 __global__ void __launch_bounds__(kNarrowThreads)
 k_levels_narrow(int l0, int l1, const int *__restrict__ lptr,
                 const int *__restrict__ rows, const int *__restrict__ rowptr,
                 const int *__restrict__ col, const int *__restrict__ diag,
-                T *lu, T *inv, T *x, int *zero_row, const int *flag,
-                const unsigned char *__restrict__ rmask, const T *src)
+                T *lu, T *inv, X *x, int *zero_row, const int *flag,
+                const unsigned char *__restrict__ rmask, const X *src)
 {
   if(flag && !*flag) return;
   for(int l = l0; l < l1; l++) {
@@ -410,20 +411,20 @@ k_levels_narrow(int l0, int l1, const int *__restrict__ lptr,
       if(MODE == 0)
         row_fact<T>(i, rowptr, col, diag, lu, inv, zero_row);
       else if(MODE == 1)
-        row_fwd<T>(i, rowptr, col, diag, lu, src, x);
+        row_fwd<T, X>(i, rowptr, col, diag, lu, src, x);
       else
-        row_bwd<T>(i, rowptr, col, diag, lu, inv, x);
+        row_bwd<T, X>(i, rowptr, col, diag, lu, inv, x);
     }
     __syncthreads();
   }
 }
 
-template <int MODE, typename T>
+template <int MODE, typename T, typename X = T>
 __global__ void __launch_bounds__(256)
 k_level_wide(int r0, int width, const int *__restrict__ rows,
              const int *__restrict__ rowptr, const int *__restrict__ col,
-             const int *__restrict__ diag, T *lu, T *inv, T *x, int *zero_row,
-             const int *flag, const unsigned char *__restrict__ rmask, const T *src)
+             const int *__restrict__ diag, T *lu, T *inv, X *x, int *zero_row,
+             const int *flag, const unsigned char *__restrict__ rmask, const X *src)
 {
   if(flag && !*flag) return;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -433,21 +434,21 @@ k_level_wide(int r0, int width, const int *__restrict__ rows,
   if(MODE == 0)
     row_fact<T>(i, rowptr, col, diag, lu, inv, zero_row);
   else if(MODE == 1)
-    row_fwd<T>(i, rowptr, col, diag, lu, src, x);
+    row_fwd<T, X>(i, rowptr, col, diag, lu, src, x);
   else
-    row_bwd<T>(i, rowptr, col, diag, lu, inv, x);
+    row_bwd<T, X>(i, rowptr, col, diag, lu, inv, x);
 }
 
 // one wide level of a triangular solve from the sliced-ELL copy: entry j
 // of the warp's 32 rows is one coalesced load (the row's entries stay in
 // CSR order, the accumulation order of lusol)
-template <int MODE, typename T>
+template <int MODE, typename T, typename X = T>
 __global__ void __launch_bounds__(256)
 k_level_ell(int r0, int w, int slice0, const int *__restrict__ rows,
             const int *__restrict__ width, const long long *__restrict__ wscan,
             const int *__restrict__ ecol, const T *__restrict__ ev,
-            const T *__restrict__ inv, T *x, const int *flag,
-            const unsigned char *__restrict__ rmask, const T *src)
+            const T *__restrict__ inv, X *x, const int *flag,
+            const unsigned char *__restrict__ rmask, const X *src)
 {
   if(flag && !*flag) return;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -457,9 +458,9 @@ k_level_ell(int r0, int w, int slice0, const int *__restrict__ rows,
   int s = slice0 + (t >> 5);
   long long e = 32 * wscan[s] + (t & 31);
   int W = width[s];
-  T acc = (MODE == 1) ? src[i] : x[i];
-  for(int j = 0; j < W; j++, e += 32) acc = acc - ev[e] * x[ecol[e]];
-  x[i] = (MODE == 2) ? inv[i] * acc : acc;
+  X acc = (MODE == 1) ? src[i] : x[i];
+  for(int j = 0; j < W; j++, e += 32) acc = acc - (X)ev[e] * x[ecol[e]];
+  x[i] = (MODE == 2) ? (X)inv[i] * acc : acc;
 }
 
 template <typename T> const T *ell_vals(const EllPart &E);
@@ -468,11 +469,11 @@ template <> const float *ell_vals<float>(const EllPart &E) { return E.v32.p; }
 
 // rmask (sweeps only): rows with rmask[i] == 0 are skipped (the rows of
 // systems of a batch that have stopped)
-template <int MODE, typename T>
+template <int MODE, typename T, typename X = T>
 // MODE 1 reads the right-hand side from src (x when null) and writes x
 static void run_levels(const gb300_matrix *A, const ilu_data *L, T *lu, T *inv,
-                       T *x, int *zero_row, const int *flag, cudaStream_t st,
-                       const unsigned char *rmask = nullptr, const T *src = nullptr)
+                       X *x, int *zero_row, const int *flag, cudaStream_t st,
+                       const unsigned char *rmask = nullptr, const X *src = nullptr)
 {
   if(!src) src = x;
   bool upper = (MODE == 2);
@@ -483,17 +484,17 @@ static void run_levels(const gb300_matrix *A, const ilu_data *L, T *lu, T *inv,
   for(size_t q = 0; q < seg.size(); q++) {
     const Segment &s = seg[q];
     if(MODE != 0 && !s.narrow && E.entries > 0) {
-      k_level_ell<MODE, T><<<grid_for(s.width, 256), 256, 0, st>>>(
+      k_level_ell<MODE, T, X><<<grid_for(s.width, 256), 256, 0, st>>>(
         s.r0, s.width, E.slice0[q], rows, E.width.p, E.wscan.p, E.col.p,
         ell_vals<T>(E), inv, x, flag, rmask, src);
       continue;
     }
     if(s.narrow)
-      k_levels_narrow<MODE, T><<<1, kNarrowThreads, 0, st>>>(
+      k_levels_narrow<MODE, T, X><<<1, kNarrowThreads, 0, st>>>(
         s.l0, s.l1, lptr, rows, A->rowptr.p, A->col.p, L->diag.p, lu, inv, x,
         zero_row, flag, rmask, src);
     else
-      k_level_wide<MODE, T><<<grid_for(s.width, 256), 256, 0, st>>>(
+      k_level_wide<MODE, T, X><<<grid_for(s.width, 256), 256, 0, st>>>(
         s.r0, s.width, rows, A->rowptr.p, A->col.p, L->diag.p, lu, inv, x,
         zero_row, flag, rmask, src);
   }
@@ -558,20 +559,29 @@ int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out,
   return GB300_OK;
 }
 
-// z = M^-1 v for the ILU(0) factor (double or float work precision)
-void ilu_apply(const gb300_matrix *A, bool fp32, const double *v, double *z,
+// z = M^-1 v for the ILU(0) factor: mode 0 FP64 factor and sweeps; 1 FP32
+// factor, sweeps on FP32 vectors in FP32 arithmetic; 2 FP32 factor, sweeps
+// in FP64 (the reference built with HAVE_ILU_FLOAT: lusol's float alu
+// against double x, ilut.F:2297-2347)
+void ilu_apply(const gb300_matrix *A, int mode, const double *v, double *z,
                float *t32, const int *flag, cudaStream_t st,
                const unsigned char *rmask)
 {
   const ilu_data *L = A->ilu;
   int n = A->n;
-  if(!fp32) {
+  if(mode == 0) {
     // the forward sweep reads v and writes z (no copy of v first); rows a
     // mask leaves out are not written
     run_levels<1, double>(A, L, (double *)L->lu64.p, (double *)L->inv64.p, z,
                           nullptr, flag, st, rmask, v);
     run_levels<2, double>(A, L, (double *)L->lu64.p, (double *)L->inv64.p, z,
                           nullptr, flag, st, rmask);
+  }
+  else if(mode == 2) {
+    run_levels<1, float, double>(A, L, (float *)L->lu32.p, (float *)L->inv32.p, z, nullptr,
+                                 flag, st, rmask, v);
+    run_levels<2, float, double>(A, L, (float *)L->lu32.p, (float *)L->inv32.p, z, nullptr,
+                                 flag, st, rmask);
   }
   else {
     k_cvt<float, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, t32, flag);
@@ -1077,6 +1087,7 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
     return GB300_ERR_ARG;
   }
   bool fp32 = (p->precision != 0);
+  const int imode = ilu_mode(p);
   if(precond) {
     int zr = 0;
     // the factor is on A's values as given to the solver (scaled if needed)
@@ -1127,7 +1138,7 @@ int gmres_solve(gb300_matrix *A, const double *val, const double *rhs,
       return;
     }
     if(precond)
-      ilu_apply(A, fp32, v, z, t32, flag, st);
+      ilu_apply(A, imode, v, z, t32, flag, st);
     else
       k_cvt<double, double><<<grid_for(n, 256), 256, 0, st>>>(n, v, z, flag);
     if(corr) correction_apply(A, val, v, z, t1, t2, flag, st);

@@ -580,7 +580,7 @@ int gmres_solve_batch(gb300_matrix *A, const double *val, const double *rhs,
   auto precond_apply = [&](const double *v, double *z, const int *flag, int which) {
     if(precond) {
       k_b_rowmask<<<gchunks, kBThreads, 0, st>>>(C, V, which, rmask.p);
-      ilu_apply(A, fp32, v, z, t32, flag, st, rmask.p);
+      ilu_apply(A, ilu_mode(p), v, z, t32, flag, st, rmask.p);
     }
     else
       k_b_copy<<<grid_for(n, 256, kReduceBlocks * 4), 256, 0, st>>>(n, v, z, flag);

@@ -638,7 +638,9 @@ int gmres_solve_batch_cluster(gb300_matrix *A, const double *val, const double *
     return GB300_OK;
   const int m = p->krylov_size <= 1 ? 15 : p->krylov_size;
   // the restart cycles are bounded by the iteration cap inside the kernel
-  if(m > kCMaxKrylov || p->nb_iter_max <= 0 || p->nb_iter_max > 100000000 || nsys < 1)
+  // (Precision 2, the FP32 factor with FP64 sweeps, takes the per-kernel form)
+  if(m > kCMaxKrylov || p->nb_iter_max <= 0 || p->nb_iter_max > 100000000 || nsys < 1 ||
+     p->precision == 2)
     return GB300_OK;
   int dev = 0, can = 0;
   GB_CUDA(cudaGetDevice(&dev));

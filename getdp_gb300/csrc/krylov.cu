@@ -826,7 +826,8 @@ int solve(gb300_matrix *A, const gb300_vector *bvec,
   if(p->algorithm == 1 && p->preconditioner != 6) {
     // CG; Preconditioner 0 and 8 (DIAGONAL stores alu = 1: the identity,
     // Sparskit.cpp:338-354) both leave the operator unchanged
-    bool mixed = (p->precision != 0);
+    // (Precision 2 concerns the ILU factor's storage only: FP64 CG here)
+    bool mixed = (p->precision == 1);
     CgState hs;
     Bsr3 B;
     bool blocked = A->block3 &&

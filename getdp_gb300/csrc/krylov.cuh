@@ -147,10 +147,19 @@ int ilu_factor(gb300_matrix *A, const double *val, bool fp32, int *zero_row_out,
                bool reuse = false, int *factorized = nullptr);
 // drop the factor held by the multicolour copy of A (a new Generate)
 void colour_drop_factor(gb300_matrix *A);
-// rmask (optional): rows with rmask[i] == 0 are left out of the sweeps
-void ilu_apply(const gb300_matrix *A, bool fp32, const double *v, double *z,
+// mode (ilu_mode): 0 FP64; 1 FP32 factor and FP32 sweeps; 2 FP32 factor,
+// FP64 sweeps (the reference's HAVE_ILU_FLOAT build); rmask (optional): rows
+// with rmask[i] == 0 are left out of the sweeps
+void ilu_apply(const gb300_matrix *A, int mode, const double *v, double *z,
                float *t32, const int *flag, cudaStream_t st,
                const unsigned char *rmask = nullptr);
+// Precision 0: FP64 ILU(0); 1: FP32 factor and FP32 sweeps (the mixed form);
+// 2: FP32 factor with FP64 sweeps, as the reference built with
+// HAVE_ILU_FLOAT (Sparskit.h:48-52) applies it
+inline int ilu_mode(const gb300_solver_params *p)
+{
+  return p->precision == 2 ? 2 : (p->precision != 0 ? 1 : 0);
+}
 
 // the Givens rotation of iters.f's givens (3235-3273): zeroes y against x;
 // x becomes the norm, (c, s) the rotation

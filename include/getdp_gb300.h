@@ -88,7 +88,11 @@ typedef struct gb300_solver_params {
   int nb_iter_max;
   double stopping_test;
   /* extensions */
-  int precision;          /* Precision: 0 FP64, 1 FP32 inner solves in FP64 refinement */
+  int precision;          /* Precision: 0 FP64, 1 FP32 inner solves in FP64
+                             refinement (CG) / the ILU(0) factor applied in
+                             FP32 (GMRES, FGMRES); 2 the ILU(0) factor stored
+                             in FP32 and applied in FP64, as the reference
+                             built with HAVE_ILU_FLOAT (Sparskit.h:48-52) */
   double inner_tolerance; /* Inner_Tolerance: mixed CG, reduction of the FP32
                              residual between two FP64 residual replacements
                              (default 0.3) */

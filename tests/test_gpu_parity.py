@@ -347,7 +347,40 @@ def test_multicolour_ilu_at_reference_tolerance():
     x = LA.LinAlg_CreateVector(None, dm.n_dof)
     info = LA.LinAlg_Solve(A, b, _solver(par), x)
     assert info["status"] == 0, info
-    assert info["true_residual"] <= 1.01e-10 * info["rhs_norm"] * 10, info
+    # GMRES stops on its Givens estimate of the residual, which drifts
+    # from the true residual in rounding (in the reference's RCMK order the
+    # GPU's true residual is within 1.01x the stopping test,
+    # test_reference_order_reproduces_the_reference_run)
+    print(f"true residual / (stopping test * ||b||): "
+          f"{info['true_residual'] / (1e-10 * info['rhs_norm']):.3f}")
+    assert info["true_residual"] <= 1.01e-10 * info["rhs_norm"], info
+    assert np.linalg.norm(x.numpy() - d["x"]) <= 1e-6 * np.linalg.norm(d["x"])
+
+
+@pytest.mark.parametrize("name", ["ms2d_n8", "ms2d_n12_dir", "ms2d_n24", "ms2d_n24_ilu32",
+                                  "eddy_n8", "eddy_n8_dir"])
+def test_reference_order_reproduces_the_reference_run(name):
+    # the golden runs of the reference binary itself, with its default RCMK
+    # order: in the same order (Renumbering_Technique 2) the GPU takes the
+    # reference's step count (+-1: classical against modified Gram-Schmidt),
+    # its true residual meets the stopping test, and the solution is the
+    # reference's within the tolerance's reach
+    d, p, dm = G.load(name)
+    par = _golden_params(d)
+    assert par["Renumbering_Technique"] == 1
+    par["Renumbering_Technique"] = 2
+    if str(d["exe"]) == "getdp_ilu32":
+        par["Precision"] = 2  # the reference built with HAVE_ILU_FLOAT
+    A = LA.LinAlg_CreateMatrix(None, dm.n_dof)
+    A.set_csr(d["indptr"], d["indices"], d["data"])
+    b = LA.LinAlg_CreateVector(None, dm.n_dof)
+    b.set(d["b"])
+    x = LA.LinAlg_CreateVector(None, dm.n_dof)
+    info = LA.LinAlg_Solve(A, b, _solver(par), x)
+    assert info["status"] == 0, info
+    assert abs(info["iterations"] - int(d["iterations"])) <= 1, (info, int(d["iterations"]))
+    rtol = float(np.float32(par["Stopping_Test"]))
+    assert info["true_residual"] <= 1.01 * rtol * info["rhs_norm"], info
     assert np.linalg.norm(x.numpy() - d["x"]) <= 1e-6 * np.linalg.norm(d["x"])
 
 
