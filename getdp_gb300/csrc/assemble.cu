@@ -13,6 +13,8 @@
 // FP64 atomic).  Fixed (Dirichlet) DOFs with values are eliminated into the
 // RHS as Dof_AssembleInMat does (DofData.cpp:1489-1542): b_i += (g_j * 1) *
 // -Ek_ij for every unknown row i and fixed column j of the element.
+#include <chrono>
+
 #include "sparse.cuh"
 
 namespace gb {
@@ -1486,11 +1488,23 @@ static int launch_elements(gb300_matrix *A, const gb300_term_batch *t, const Bat
   return GB300_OK;
 }
 
+// max |v_i| as the bits of a non-negative double (ordered as integers):
+// per thread over a grid stride, per warp by shuffles, one atomic per warp
+// (an atomic per entry on the one address had cost ~150 ms at 229 M entries)
 __global__ void k_absmax_bits(long long n, const double *__restrict__ v,
                               unsigned long long *__restrict__ out)
 {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if(i < n) atomicMax(out, (unsigned long long)__double_as_longlong(fabs(v[i])));
+  unsigned long long m = 0;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+      i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(v[i]));
+    m = b > m ? b : m;
+  }
+  for(int o = 16; o > 0; o >>= 1) {
+    const unsigned long long u = __shfl_down_sync(0xffffffffu, m, o);
+    m = u > m ? u : m;
+  }
+  if((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
 __global__ void k_differs(long long n, const double *__restrict__ a,
@@ -1505,10 +1519,20 @@ __global__ void k_differs(long long n, const double *__restrict__ a,
 // result against the warp-per-element kernel's (shape 0; 1e-12 of the
 // largest entry: the shapes differ only in the order of the additions) and
 // keeps the fastest shape that agrees in the cache entry
+// host time of the first Generate's one-off steps (GB300_TUNE_VERBOSE)
+static double now_ms()
+{
+  return std::chrono::duration<double, std::milli>(
+           std::chrono::steady_clock::now().time_since_epoch())
+    .count();
+}
+
 static int tune_shape(gb300_matrix *A, GenCache *G, const gb300_term_batch *t,
                       const BatchDev &B, const gb300_vector *x, const int *pairpos, int mode,
                       cudaStream_t st)
 {
+  const bool verbose = getenv("GB300_TUNE_VERBOSE") != nullptr;
+  const double t0 = verbose ? now_ms() : 0.;
   const int n_l = t->n_elems < kTuneElements ? t->n_elems : kTuneElements;
   const long long nnz = A->nnz > 0 ? A->nnz : 1;
   DevBuf<double> sval, rval, sb, rb;
@@ -1522,6 +1546,10 @@ static int tune_shape(gb300_matrix *A, GenCache *G, const gb300_term_batch *t,
   GB_TRY(bad.alloc(1));
   GB_TRY(amax.alloc(1));
   GB_CUDA(cudaMemsetAsync(serr.p, 0, sizeof(int), st));
+  if(verbose) {
+    GB_CUDA(cudaStreamSynchronize(st));
+    fprintf(stderr, "element tuner: scratch allocated in %.2f ms\n", now_ms() - t0);
+  }
   CsrView S{A->rowptr.p, A->col.p, sval.p, serr.p};
   // the coloured scatter's element lists are per colour: tune the same
   // kernels with atomics on the prefix (the arithmetic is the same)
@@ -1544,7 +1572,8 @@ static int tune_shape(gb300_matrix *A, GenCache *G, const gb300_term_batch *t,
     unsigned long long h = 0;
     GB_CUDA(cudaMemsetAsync(amax.p, 0, sizeof(h), st));
     const long long m = k ? (A->n > 0 ? A->n : 1) : nnz;
-    k_absmax_bits<<<grid_for(m, 256), 256, 0, st>>>(m, k ? rb.p : rval.p, amax.p);
+    k_absmax_bits<<<grid_for(m, 256, kReduceBlocks * 4), 256, 0, st>>>(m, k ? rb.p : rval.p,
+                                                                       amax.p);
     GB_CUDA(cudaMemcpyAsync(&h, amax.p, sizeof(h), cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
     memcpy(k ? &bmax : &vmax, &h, sizeof(double));
@@ -1589,6 +1618,7 @@ static int tune_shape(gb300_matrix *A, GenCache *G, const gb300_term_batch *t,
     return GB300_ERR_ARG;
   }
   G->shape = bests;
+  if(verbose) fprintf(stderr, "element tuner: %.2f ms in all\n", now_ms() - t0);
   return GB300_OK;
 }
 
@@ -1645,7 +1675,10 @@ int generate_values(gb300_matrix *A, gb300_vector *b, const gb300_term_batch *t,
   }
   const int *pairpos = nullptr;
   if(ne > 0 && table_ok && mode != GB300_SCATTER_SEARCH) {
+    const bool verbose = getenv("GB300_TUNE_VERBOSE") != nullptr && !G->pairpos_ok;
+    const double t0 = verbose ? now_ms() : 0.;
     GB_TRY(ensure_pairpos(A, G));
+    if(verbose) fprintf(stderr, "position table: %.2f ms\n", now_ms() - t0);
     pairpos = G->pairpos.p;
   }
   const bool coloured = (mode == GB300_SCATTER_COLOURED);

@@ -772,13 +772,23 @@ __global__ void k_tune_check(size_t n4, const T *q, const T *ref, double scale,
   if(!(d <= tol * scale)) atomicExch(bad, 1);
 }
 
+// max |q_i| (bits of a non-negative double): grid stride, warp shuffles,
+// one atomic per warp
 template <typename T>
 __global__ void k_absmax(size_t n4, const T *q, unsigned long long *out)
 {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if(i >= n4) return;
-  double v = fabs((double)q[i]);
-  atomicMax(out, (unsigned long long)__double_as_longlong(v));
+  unsigned long long m = 0;
+  for(size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4;
+      i += (size_t)gridDim.x * blockDim.x) {
+    const unsigned long long b =
+      (unsigned long long)__double_as_longlong(fabs((double)q[i]));
+    m = b > m ? b : m;
+  }
+  for(int o = 16; o > 0; o >>= 1) {
+    const unsigned long long u = __shfl_down_sync(0xffffffffu, m, o);
+    m = u > m ? u : m;
+  }
+  if((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
 // Times every launch shape on this matrix (alternating between two input
@@ -804,7 +814,8 @@ static int tune_one(Bsr3 &B, const T *val, int *out, cudaStream_t st)
   // the reference: the plain (non-staged) kernel, variant 1
   launch_bsr<2, T>(1, B, val, pa.p, nullptr, qref.p, part.p, nullptr, st);
   GB_CUDA(cudaMemsetAsync(amax.p, 0, sizeof(unsigned long long), st));
-  k_absmax<T><<<grid_for((long long)n4, 256), 256, 0, st>>>(n4, qref.p, amax.p);
+  k_absmax<T><<<grid_for((long long)n4, 256, kReduceBlocks * 4), 256, 0, st>>>(n4, qref.p,
+                                                                                amax.p);
   unsigned long long hmax = 0;
   GB_CUDA(cudaMemcpyAsync(&hmax, amax.p, sizeof(hmax), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));
