@@ -507,6 +507,7 @@ int gb300_matrix_add_coo(gb300_matrix *A, long long count, const int *i,
 
 int gb300_matrix_assemble(gb300_matrix *A)
 {
+  gb::NvtxRange nvtx_range("gb300_matrix_assemble");
   GB_TRY(check(A, "matrix"));
   if(A->hr.empty() && A->csr_valid) return GB300_OK;
   cudaStream_t st = A->ctx->stream;
@@ -678,6 +679,7 @@ int gb300_matrix_mult(gb300_matrix *A, const gb300_vector *x, gb300_vector *y)
 // -------------------------------------------------------------- generate
 int gb300_generate_pattern(gb300_matrix *A, const gb300_term_batch *t)
 {
+  gb::NvtxRange nvtx_range("gb300_generate_pattern");
   GB_TRY(check(A, "matrix"));
   GB_TRY(check(t, "term batch"));
   // a Generate makes a new matrix (GetDP's ZeroMatrix): no factor survives it
@@ -692,6 +694,7 @@ int gb300_generate_pattern(gb300_matrix *A, const gb300_term_batch *t)
 int gb300_generate_values(gb300_matrix *A, gb300_vector *b,
                           const gb300_term_batch *t)
 {
+  gb::NvtxRange nvtx_range("gb300_generate_values");
   GB_TRY(check(A, "matrix"));
   GB_TRY(check(b, "rhs"));
   GB_TRY(check(t, "term batch"));
@@ -701,6 +704,7 @@ int gb300_generate_values(gb300_matrix *A, gb300_vector *b,
 int gb300_generate_values_at(gb300_matrix *A, gb300_vector *b,
                              const gb300_term_batch *t, const gb300_vector *x)
 {
+  gb::NvtxRange nvtx_range("gb300_generate_values_at");
   GB_TRY(check(A, "matrix"));
   GB_TRY(check(b, "rhs"));
   GB_TRY(check(t, "term batch"));
@@ -858,6 +862,7 @@ int gb300_solve(gb300_matrix *A, const gb300_vector *b,
                 const gb300_solver_params *p, gb300_vector *x,
                 gb300_solve_info *info)
 {
+  gb::NvtxRange nvtx_range("gb300_solve");
   GB_TRY(check(A, "matrix"));
   GB_TRY(check(b, "rhs"));
   GB_TRY(check(p, "params"));
@@ -944,6 +949,7 @@ int gb300_matrix_scale_correction(gb300_matrix *A, double s)
 int gb300_precond_apply(gb300_matrix *A, const gb300_solver_params *p,
                         const gb300_vector *v, gb300_vector *z)
 {
+  gb::NvtxRange nvtx_range("gb300_precond_apply");
   GB_TRY(check(A, "matrix"));
   GB_TRY(check(p, "params"));
   GB_TRY(check(v, "v"));
@@ -959,6 +965,7 @@ int gb300_precond_apply(gb300_matrix *A, const gb300_solver_params *p,
 int gb300_post_elements(const gb300_term_batch *t, const gb300_vector *x,
                         double *out)
 {
+  gb::NvtxRange nvtx_range("gb300_post_elements");
   GB_TRY(check(t, "term batch"));
   GB_TRY(check(x, "solution"));
   GB_TRY(check(out, "out"));
@@ -968,6 +975,7 @@ int gb300_post_elements(const gb300_term_batch *t, const gb300_vector *x,
 int gb300_post_points(const gb300_term_batch *t, const gb300_vector *x, int npts,
                       const double *xyz, double *field, double *curl, int *elem)
 {
+  gb::NvtxRange nvtx_range("gb300_post_points");
   GB_TRY(check(t, "term batch"));
   GB_TRY(check(x, "solution"));
   if(npts > 0) GB_TRY(check(xyz, "xyz"));
@@ -1002,6 +1010,7 @@ int gb300_solve_batch(gb300_matrix *A, const gb300_vector *b,
                       const gb300_solver_params *p, gb300_vector *x, int nsys,
                       const int *offsets, gb300_solve_info *infos)
 {
+  gb::NvtxRange nvtx_range("gb300_solve_batch");
   GB_TRY(check(A, "matrix"));
   GB_TRY(check(b, "rhs"));
   GB_TRY(check(p, "params"));

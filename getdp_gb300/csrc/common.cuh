@@ -2,6 +2,7 @@
 // (one device, one stream), device buffers and small device helpers.
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 
 #include <cstdarg>
@@ -13,6 +14,17 @@
 #include "../../include/getdp_gb300.h"
 
 namespace gb {
+
+// NVTX range over a scope: the C ABI's phases (Generate, solve, batched
+// solve, post-processing, network) show up by name in ncu / Nsight captures
+// (ncu --nvtx --nvtx-include "gb300_solve/"); a no-op without a tool
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 
 struct ilu_data;
 struct Colouring;

@@ -24,10 +24,12 @@
 // let the correction add oscillatory components that A amplifies; the
 // energy norm weighs them as the Krylov iteration does.
 //
-// Kernels: one warp per node (lane = channel) for the layers and the output
-// head; weight gradients accumulate per warp in registers and are added
-// with FP32 atomics (their order varies, so gradients agree with the FP64
-// CPU check to FP32 rounding, not bit for bit).
+// Kernels: the forward layers on the tensor cores over 16-node tiles
+// (k_mp_layer_mma); one warp per node (lane = channel) for the input, the
+// output head and the backward pass; weight gradients accumulate per warp in
+// registers and are added with FP32 atomics (their order varies, so
+// gradients agree with the FP64 CPU check to FP32 rounding, not bit for
+// bit).
 #include <cuda_bf16.h>
 
 #include <random>
@@ -152,47 +154,14 @@ k_mp_input(int n, const float *__restrict__ feat, const float *__restrict__ wq,
   }
 }
 
-// one message-passing layer: m_i = sum_{j != i} e_ij h_j,
-// h'_i = relu(W_s h_i + W_n m_i + b)
-__global__ void __launch_bounds__(32 * kNodeWarps)
-k_mp_layer(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
-           const float *__restrict__ ehat, const float *__restrict__ wl,
-           const float *__restrict__ hin, float *__restrict__ mout,
-           float *__restrict__ hout)
-{
-  __shared__ float Ws[kH][kH + 1], Wn[kH][kH + 1];
-  for(int t = threadIdx.x; t < kH * kH; t += blockDim.x) {
-    Ws[t / kH][t % kH] = wl[t];
-    Wn[t / kH][t % kH] = wl[kH * kH + t];
-  }
-  __syncthreads();
-  const float bias = wl[2 * kH * kH + (threadIdx.x & 31)];
-  int lane = threadIdx.x & 31;
-  for(int i = blockIdx.x * kNodeWarps + (threadIdx.x >> 5); i < n;
-      i += gridDim.x * kNodeWarps) {
-    float mi = 0.f;
-    for(int k = rowptr[i]; k < rowptr[i + 1]; k++) {
-      int j = col[k];
-      if(j != i) mi += ehat[k] * hin[(size_t)j * kH + lane];
-    }
-    float hi = hin[(size_t)i * kH + lane];
-    float z = bias;
-#pragma unroll
-    for(int d = 0; d < kH; d++) {
-      float hd = __shfl_sync(0xffffffffu, hi, d);
-      float md = __shfl_sync(0xffffffffu, mi, d);
-      z += Ws[lane][d] * hd + Wn[lane][d] * md;
-    }
-    mout[(size_t)i * kH + lane] = mi;
-    hout[(size_t)i * kH + lane] = fmaxf(z, 0.f);
-  }
-}
-
-// The same layer with its dense part on the tensor cores (mma.sync
-// m16n8k16, BF16 in, FP32 accumulation).  The kernel above is bound by its
-// load/store pipe: every lane broadcasts its channel by shuffle and reads a
-// row of the two 32 x 32 weight matrices from shared memory, 64 of each per
-// node and layer for 64 FMAs.  Here a warp takes 16 nodes at a time: it sums
+// One message-passing layer, m_i = sum_{j != i} e_ij h_j,
+// h'_i = relu(W_s h_i + W_n m_i + b), with its dense part on the tensor
+// cores (mma.sync m16n8k16, BF16 in, FP32 accumulation).  A warp-per-node
+// form on the CUDA cores (lane = channel) was bound by its load/store pipe:
+// every lane broadcast its channel by shuffle and read a row of the two
+// 32 x 32 weight matrices from shared memory, 64 of each per node and layer
+// for 64 FMAs (649 us per layer at 1024^2 against 241 us here).  Here a
+// warp takes 16 nodes at a time: it sums
 // their messages as above (lane = channel) into a 16 x 64 shared tile
 // [h | m], then multiplies the tile by [W_s | W_n]^T held in registers as
 // BF16 MMA operands (the weights are BF16-rounded already: exact).  The
@@ -252,7 +221,7 @@ k_mp_layer_mma(int n, const int *__restrict__ rowptr, const int *__restrict__ co
     // messages of the tile's 16 nodes: lane = (node r, half hf of the
     // channels), each neighbour's 16 channels gathered as four float4, so a
     // warp walks its 16 rows side by side (each channel summed in the row's
-    // order, as in k_mp_layer)
+    // order)
     {
       const int r = lane >> 1, hf = lane & 1;
       const int i = 16 * t + r;
@@ -787,6 +756,7 @@ int gb300_mpnn_get_params(const gb300_mpnn *net, float *host)
 
 int gb300_mpnn_infer(gb300_mpnn *net, gb300_matrix *A)
 {
+  gb::NvtxRange nvtx_range("gb300_mpnn_infer");
   if(!net || !A) {
     set_error("network: null argument");
     return GB300_ERR_ARG;
@@ -806,6 +776,7 @@ int gb300_mpnn_loss_grad(gb300_mpnn *net, gb300_matrix *A, const gb300_vector *r
                          const gb300_vector *e1, int accumulate, double *loss,
                          float *grad_host)
 {
+  gb::NvtxRange nvtx_range("gb300_mpnn_loss_grad");
   if(!net || !A || !r1 || !loss) {
     set_error("network: null argument");
     return GB300_ERR_ARG;
@@ -845,6 +816,7 @@ int gb300_mpnn_set_loss(gb300_mpnn *net, int mode)
 
 int gb300_mpnn_adam_step(gb300_mpnn *net, float lr, float grad_scale)
 {
+  gb::NvtxRange nvtx_range("gb300_mpnn_adam_step");
   if(!net) {
     set_error("network: null argument");
     return GB300_ERR_ARG;
