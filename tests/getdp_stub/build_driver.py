@@ -32,13 +32,17 @@ def prototypes(text: str) -> str:
 def build() -> str:
     from getdp_gb300 import build as B
     lib = B.build()
+    srcs = [BACKEND, os.path.join(HERE, "stub.cpp"), os.path.join(HERE, "drive_linalg.cpp")]
+    deps = srcs + [lib, os.path.join(ROOT, "include", "getdp_gb300.h")] + \
+        [os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith(".h")]
+    if os.path.exists(EXE) and os.path.getmtime(EXE) >= max(os.path.getmtime(d) for d in deps):
+        return EXE
     os.makedirs(OUT, exist_ok=True)
     with open(BACKEND) as f:
         protos = prototypes(f.read())
     hdr = os.path.join(OUT, "linalg_protos.h")
     with open(hdr, "w") as f:
         f.write("/* generated from LinAlg_GB300.cpp */\n" + protos)
-    srcs = [BACKEND, os.path.join(HERE, "stub.cpp"), os.path.join(HERE, "drive_linalg.cpp")]
     cmd = ["g++", "-O2", "-std=c++17", "-w", "-I", OUT, "-I", HERE,
            "-I", os.path.join(ROOT, "include"), *srcs, "-o", EXE,
            "-L", os.path.dirname(lib), "-lgetdp_gb300",
