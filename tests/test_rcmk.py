@@ -94,3 +94,27 @@ def test_rcmk_solve_follows_the_reference_default(algorithm):
     S.set("Renumbering_Technique", 1)
     info1 = LA.LinAlg_Solve(A, b, S, x)
     print(f"RCMK {info['iterations']} (oracle {its}), multicolour {info1['iterations']}")
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_rcmk_order_random_symmetric_patterns(seed):
+    # random structurally symmetric patterns with a full diagonal, some in
+    # several components and with isolated rows: the order equals the
+    # restated cmkreord's permutation
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(1, 400))
+    m = int(rng.integers(0, 4 * n))
+    i = rng.integers(0, n, m)
+    j = rng.integers(0, n, m)
+    if seed % 2:  # two diagonal blocks: no entry couples them
+        cut = n // 2
+        keep = (i < cut) == (j < cut)
+        i, j = i[keep], j[keep]
+    import scipy.sparse as sp
+    S = sp.coo_matrix((np.ones(len(i)), (i, j)), shape=(n, n))
+    S = (S + S.T + sp.eye(n)).tocsr()
+    S.sort_indices()
+    ip, ix = S.indptr.astype(np.int32), S.indices.astype(np.int32)
+    got = _order(ip, ix)
+    want = oracle.rcmk_new_of(ip, ix)
+    assert np.array_equal(got, want)
