@@ -88,6 +88,8 @@ def parse():
                     help="nonlinear: cells per side of the aggregates of the two-level "
                          "preconditioner (Preconditioner 21); 0: aggregates from the "
                          "matrix graph")
+    ap.add_argument("--two-level-only", action="store_true",
+                    help="nonlinear workload: only the two-level (and learned) arms")
     ap.add_argument("--learned-two-level-weights", default=None,
                     help="nonlinear workload: also time the Newton loop with the correction "
                          "trained for the two-level cycle (Preconditioner 22, .npy)")
@@ -832,7 +834,7 @@ def run_nonlinear(args, ws, rank, local):
         return d, out
 
     res = {}
-    for prec in (0, 1):
+    for prec in (() if args.two_level_only else (0, 1)):
         run_gpu(n, prec, 1)  # warm-up (pattern, colouring, tuning)
         res[prec], _ = run_gpu(n, prec, max(args.steps, 1))
     two = {}
@@ -842,14 +844,16 @@ def run_nonlinear(args, ws, rank, local):
     best = min(list(res.values()) + list(two.values()), key=lambda r: r["s"])
     # the same with the coloured (atomic-free) scatter: Generate, and so the
     # whole Newton loop, gives the same numbers on every run
-    det = []
-    for _ in range(2):
-        r, o = run_gpu(n, 1, 1, scatter=_lib.SCATTER_COLOURED)
-        det.append((r, float(o.history[-1])))
-    deterministic = dict(det[1][0])
-    deterministic["repeat_identical"] = bool(
-        det[0][0]["linear_iterations"] == det[1][0]["linear_iterations"] and
-        det[0][1] == det[1][1])
+    deterministic = None
+    if not args.two_level_only:
+        det = []
+        for _ in range(2):
+            r, o = run_gpu(n, 1, 1, scatter=_lib.SCATTER_COLOURED)
+            det.append((r, float(o.history[-1])))
+        deterministic = dict(det[1][0])
+        deterministic["repeat_identical"] = bool(
+            det[0][0]["linear_iterations"] == det[1][0]["linear_iterations"] and
+            det[0][1] == det[1][1])
     learned = None
     if args.learned_weights:
         from getdp_gb300 import learned as LR
@@ -891,7 +895,7 @@ def run_nonlinear(args, ws, rank, local):
                     "learned_attempt_iterations": int(sum(
                         s.get("learned_attempt_iterations") or 0 for s in pol.log)),
                     "solves": pol.log, "converged": r.converged, "aggregates": nc,
-                    "speedup_vs_plain_fp64": res[0]["s"] / t_l,
+                    "speedup_vs_plain_fp64": res[0]["s"] / t_l if 0 in res else None,
                     "speedup_vs_two_level_mixed": two[1]["s"] / t_l,
                     "weights": os.path.basename(args.learned_two_level_weights)}
     line = {"metric": "nonlinear 2D magnetostatics: time to 1e-8 Newton residual "
@@ -905,11 +909,12 @@ def run_nonlinear(args, ws, rank, local):
                                    "Newton, ILU(0)-(F)GMRES(50) per step; two-level "
                                    "arms: ILU(0) around a coarse correction on "
                                    f"{args.coarse_cells}^2 cells (Preconditioner 21)",
-                       "elements": 2 * n * n, "unknowns": res[0]["unknowns"],
+                       "elements": 2 * n * n, "unknowns": two[0]["unknowns"],
                        "parallelism": f"replicas x{ws}"},
-            "fp64": res[0], "mixed": res[1], "two_level_fp64": two[0],
+            "fp64": res.get(0), "mixed": res.get(1), "two_level_fp64": two[0],
             "two_level_mixed": two[1],
-            "speedup_two_level_mixed_vs_plain_fp64": res[0]["s"] / two[1]["s"],
+            "speedup_two_level_mixed_vs_plain_fp64":
+                res[0]["s"] / two[1]["s"] if 0 in res else None,
             "mixed_coloured_scatter": deterministic}
     if learned is not None:
         line["learned_mixed"] = learned
