@@ -438,9 +438,11 @@ int gb300_rcmk_order(int n, const int *rowptr, const int *col, int *new_of);
    array); an entry coupling two blocks is an error.  Each system is solved
    as gb300_solve would solve it alone (GMRES or FGMRES, Preconditioner 0 or
    6; Renumbering_Technique 1 reorders within each block), with its own
-   convergence test, iteration count and status in infos[k] (nsys entries);
-   all of them share every kernel launch.  Returns GB300_ERR_SOLVER (with
-   the solutions and infos filled) if any system did not converge. */
+   convergence test, iteration count and status in infos[k] (nsys entries).
+   By default the whole batch is one launch, a thread-block cluster per
+   system (Batch_Kernel, infos[k].batch_form = 1); otherwise every Krylov
+   kernel launch serves all systems.  Returns GB300_ERR_SOLVER (with the
+   solutions and infos filled) if any system did not converge. */
 int gb300_solve_batch(gb300_matrix *A, const gb300_vector *b,
                       const gb300_solver_params *p, gb300_vector *x, int nsys,
                       const int *offsets, gb300_solve_info *infos);
