@@ -146,6 +146,10 @@ SIGNATURES = {
     "gb300_post_elements": (_I, [ctypes.POINTER(TermBatch), _P, _P]),
     "gb300_post_points": (_I, [ctypes.POINTER(TermBatch), _P, _I, _P, _P, _P, _P]),
     "gb300_rcmk_order": (_I, [_I, _P, _P, _P]),
+    "gb300_format_dof_records": (_I, [ctypes.c_longlong, _P, _P, _P, ctypes.c_longlong,
+                                      ctypes.POINTER(ctypes.c_longlong)]),
+    "gb300_format_int_rows": (_I, [ctypes.c_longlong, _I, _P, ctypes.c_longlong, _P,
+                                   ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]),
     "gb300_solve_batch": (_I, [_P, _P, ctypes.POINTER(SolverParams), _P, _I,
                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(SolveInfo)]),
     "gb300_event_record": (_I, [_P, _I]),

@@ -236,26 +236,33 @@ def dof_records(mesh, dm):
         numtype = np.broadcast_to(comp + 1, (ne, nloc)).ravel()
         flat = ed.ravel()
         harm = [(h, flat) for h in range(dm.nharm)]
-    recs = []
-    for h, d in harm:
-        unk = d >= 0
-        num = np.where(unk, d + h + 1, 0)  # 1-based; harmonic 1 is the next number
-        if fv is None:
-            val = np.zeros(len(d))
+    # one occurrence of each (NumType, Entity) the tables touch, in key order:
+    # the keys are dense, so an index over their range replaces a sort (any
+    # occurrence will do: every occurrence of a DOF carries the same number)
+    numtype = np.ascontiguousarray(numtype, np.int64)
+    if len(ent) == 0:
+        return np.zeros((0, 6))
+    span_e = int(ent.max()) + 1
+    key = numtype * span_e + ent
+    idx = np.full(int(key.max()) + 1, -1, np.int64)
+    idx[key] = np.arange(len(key))
+    sel = idx[idx >= 0]
+    nh = len(harm)
+    sel = np.repeat(sel, nh)  # harmonics of one DOF next to each other
+    h = np.tile(np.arange(nh), len(sel) // nh)
+    d = flat[sel]
+    unk = d >= 0
+    num = np.where(unk, d + h + 1, 0)  # 1-based; harmonic 1 is the next number
+    if fv is None:
+        val = np.zeros(len(d))
+    else:
+        k = np.maximum(-d - 1, 0)
+        if fv.ndim == 2:
+            val = fv[k, h]
         else:
-            k = np.maximum(-d - 1, 0)
-            val = fv[k, h] if fv.ndim == 2 else (fv[k] if h == 0 else np.zeros(len(d)))
-            val = np.where(unk, 0.0, val)
-        recs.append(np.stack([numtype, ent, np.full(len(d), h), np.where(unk, 1, 2),
-                              num, val], 1))
-    r = np.concatenate(recs)
-    # (NumType, Entity, Harmonic) order as one integer key
-    ki = r[:, :3].astype(np.int64)
-    span_e = int(ki[:, 1].max()) + 1 if len(ki) else 1
-    span_h = int(ki[:, 2].max()) + 1 if len(ki) else 1
-    key = (ki[:, 0] * span_e + ki[:, 1]) * span_h + ki[:, 2]
-    _, first = np.unique(key, return_index=True)
-    return r[first]
+            val = np.where(h == 0, fv[k], 0.0)
+        val = np.where(unk, 0.0, val)
+    return np.stack([numtype[sel], ent[sel], h, np.where(unk, 1, 2), num, val], 1)
 
 
 def write_pre(path: str, mesh, dm, resolution: str = "R", n_spaces: int = None) -> None:
@@ -268,28 +275,74 @@ def write_pre(path: str, mesh, dm, resolution: str = "R", n_spaces: int = None) 
     if n_spaces is None:
         n_spaces = int(r[:, 0].max()) if len(r) else 1
     n_unknown = int(np.sum(r[:, 3] == 1))
-    out = [f"$Resolution /* '{resolution}' */", "0 1", "$EndResolution",
-           "$DofData /* #0 */", "0 0",
-           " ".join([str(n_spaces)] + [str(i) for i in range(n_spaces)]),
-           "1 0", "1 0", f"{len(r)} {n_unknown}"]
-    ints = r[:, :5].astype(np.int64).tolist()
-    vals = r[:, 5].tolist()
-    out.extend(f"{nt} {ent} {h} 1 {num} 1" if typ == 1 else
-               f"{nt} {ent} {h} 2 {'%.16g' % v} 0"
-               for (nt, ent, h, typ, num), v in zip(ints, vals))
-    out.append("$EndDofData")
-    if dm.edges is not None:
-        out.extend(_elements_x_edges(mesh, dm))
-    with open(path, "w") as f:
-        f.write("\n".join(out) + "\n")
+    head = [f"$Resolution /* '{resolution}' */", "0 1", "$EndResolution",
+            "$DofData /* #0 */", "0 0",
+            " ".join([str(n_spaces)] + [str(i) for i in range(n_spaces)]),
+            "1 0", "1 0", f"{len(r)} {n_unknown}"]
+    L = _native()
+    with open(path, "wb") as f:
+        f.write(("\n".join(head) + "\n").encode())
+        if L is not None:
+            rec5 = np.ascontiguousarray(r[:, :5], np.int64)
+            vals = np.ascontiguousarray(r[:, 5], np.float64)
+            f.write(_native_text(L.gb300_format_dof_records, len(r), 160,
+                                 rec5, vals))
+        else:
+            ints = r[:, :5].astype(np.int64).tolist()
+            f.write("".join(f"{nt} {ent} {h} 1 {num} 1\n" if typ == 1 else
+                            f"{nt} {ent} {h} 2 {'%.16g' % v} 0\n"
+                            for (nt, ent, h, typ, num), v in
+                            zip(ints, r[:, 5].tolist())).encode())
+        f.write(b"$EndDofData\n")
+        if dm.edges is not None:
+            _write_elements_x_edges(f, mesh, dm, L)
 
 
-def _elements_x_edges(mesh, dm):
+def _native():
+    """The library's text formatters, where the library is built (the
+    formatting in Python below gives the same bytes)."""
+    try:
+        from . import _lib
+        return _lib.load()
+    except (ImportError, OSError):
+        return None
+
+
+def _native_text(fn, nrows: int, per_row: int, *args) -> bytes:
+    import ctypes
+    from . import _lib
+    cap = nrows * per_row + 64
+    buf = np.empty(cap, np.uint8)
+    n = ctypes.c_longlong(0)
+    ptrs = [a.ctypes.data_as(ctypes.c_void_p) if isinstance(a, np.ndarray) else a for a in args]
+    _lib.check(fn(nrows, *ptrs, buf.ctypes.data_as(ctypes.c_void_p), cap, ctypes.byref(n)))
+    return buf[:n.value].tobytes()
+
+
+def _write_elements_x_edges(f, mesh, dm, L):
     """$ElementsXEdges (Geo_WriteFilePRE, GeoEntity.cpp:526-552): every
     element with edges, in mesh order (volume elements, then the boundary
     elements whose edges the constraint created), with its edges' numbers,
     negative where the element runs the edge from the higher to the lower
     node number (GeoEntity.h:214-215 local edges)."""
+    blocks = _edge_blocks(mesh, dm)
+    if L is None:
+        f.write(("\n".join(_elements_x_edges(blocks)) + "\n").encode())
+        return
+    import ctypes
+    f.write(f"$ElementsXEdges\n0 {sum(len(b) for b in blocks)}\n".encode())
+    i = 0
+    for blk in blocks:
+        v = np.ascontiguousarray(blk, np.int64)
+        f.write(_native_text(L.gb300_format_int_rows, len(v), 40 + 21 * v.shape[1],
+                             ctypes.c_int(v.shape[1]), v, ctypes.c_longlong(i)))
+        i += len(v)
+    f.write(b"$EndElementsXEdges\n")
+
+
+def _edge_blocks(mesh, dm):
+    """The signed edge numbers of every element with edges (volume
+    elements, then boundary elements), one array per element kind."""
     from .workloads import TET4_EDGES, TRI3_EDGES_GETDP
     nn = mesh.n_nodes
     ekey = dm.edges[:, 0].astype(np.int64) * nn + dm.edges[:, 1]
@@ -304,6 +357,11 @@ def _elements_x_edges(mesh, dm):
     blocks = [signed(mesh.elems, TET4_EDGES)]
     if len(mesh.bnd):
         blocks.append(signed(mesh.bnd, TRI3_EDGES_GETDP))
+    return blocks
+
+
+def _elements_x_edges(blocks):
+    """The $ElementsXEdges block as text lines (the Python formatting)."""
     lines = ["$ElementsXEdges", f"0 {sum(len(b) for b in blocks)}"]
     i = 0
     for blk in blocks:

@@ -425,6 +425,20 @@ int gb300_solve(gb300_matrix *A, const gb300_vector *b,
                 const gb300_solver_params *p, gb300_vector *x,
                 gb300_solve_info *info);
 
+/* Text of the two bulky blocks of a .pre file, into a caller's buffer of
+   cap bytes (*len: bytes written; GB300_ERR_CAPACITY if cap is too small);
+   host only.  gb300_format_dof_records: the $DofData records of
+   Dof_WriteFilePRE (DofData.cpp:363-462), rec5[5 i..5 i+4] = (NumType,
+   Entity, Harmonic, Type, NumDof): "NumType Entity Harmonic 1 NumDof 1" for
+   Type 1 (unknown), else "NumType Entity Harmonic 2 val[i] 0" with val[i]
+   as "%.16g" (LinAlg_PrintScalar).  gb300_format_int_rows: the
+   $ElementsXEdges rows of Geo_WriteFilePRE (GeoEntity.cpp:526-552),
+   "index width v_1 .. v_width" for rows numbered from first_index. */
+int gb300_format_dof_records(long long n, const long long *rec5, const double *val,
+                             char *out, long long cap, long long *len);
+int gb300_format_int_rows(long long nrows, int width, const long long *vals,
+                          long long first_index, char *out, long long cap, long long *len);
+
 /* The reverse Cuthill-McKee order Sparskit computes for Renumbering_Technique
    1 (cmkreord, contrib/Sparskit/cmkreord.f:3-30, called at
    Sparskit.cpp:247-250): new_of[i] is the new index of row i of the n x n

@@ -158,3 +158,37 @@ def test_pre_writer_round_trips_the_numbering(tmp_path):
         key = [(k // nv + 1, int(v) + 1) for v in p.mesh.elems[:, k % nv]]
         got = np.array([num.get(kk, -1) for kk in key])
         assert np.array_equal(got, np.where(dm.elem_dofs[:, k] >= 0, dm.elem_dofs[:, k], -1))
+
+
+def test_native_pre_formatting_equals_python():
+    """The library's formatters of the .pre blocks give the bytes of the
+    Python formatting (records of both types, "%.16g" of awkward values,
+    signed edge rows), and refuse a buffer that is too small."""
+    import ctypes
+    from getdp_gb300 import _lib
+    L = _lib.load(build_if_missing=True)
+    rng = np.random.default_rng(3)
+    vals = np.concatenate([[0.0, -0.0, 1.0, -1.5, 1e-300, -2.5e-308, 1e300, np.pi,
+                            1 / 3, 123456789.0123456789, 5e-5, 1e16, 1e15 + 0.5],
+                           rng.standard_normal(200) * 10.0 ** rng.integers(-20, 20, 200)])
+    n = len(vals)
+    rec5 = np.column_stack([rng.integers(1, 4, n), rng.integers(1, 10 ** 9, n),
+                            rng.integers(0, 2, n), rng.integers(1, 3, n),
+                            rng.integers(1, 10 ** 7, n)]).astype(np.int64)
+    got = FIO._native_text(L.gb300_format_dof_records, n, 160, rec5, vals)
+    want = "".join(f"{nt} {ent} {h} 1 {num} 1\n" if typ == 1 else
+                   f"{nt} {ent} {h} 2 {'%.16g' % v} 0\n"
+                   for (nt, ent, h, typ, num), v in zip(rec5.tolist(), vals.tolist()))
+    assert got == want.encode()
+    rows = rng.integers(-10 ** 6, 10 ** 6, (50, 6)).astype(np.int64)
+    got = FIO._native_text(L.gb300_format_int_rows, len(rows), 40 + 21 * 6,
+                           ctypes.c_int(6), rows, ctypes.c_longlong(7))
+    want = "".join(f"{7 + i} 6 " + " ".join(map(str, r)) + "\n"
+                   for i, r in enumerate(rows.tolist()))
+    assert got == want.encode()
+    buf = np.empty(8, np.uint8)
+    m = ctypes.c_longlong(0)
+    rc = L.gb300_format_dof_records(n, rec5.ctypes.data_as(ctypes.c_void_p),
+                                    vals.ctypes.data_as(ctypes.c_void_p),
+                                    buf.ctypes.data_as(ctypes.c_void_p), 8, ctypes.byref(m))
+    assert rc == 6  # GB300_ERR_CAPACITY
